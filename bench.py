@@ -1,0 +1,393 @@
+#!/usr/bin/env python
+"""Benchmark of the vorticity-streamfunction time step on GB300.
+
+Workload (one "step" = one explicit time step of cnavier's solver, src/main.c:283-395): the
+lid-driven cavity on a 1024 x 1024 grid, Re = 1000, lid u = 1, w = psi = 0 at t = 0,
+dt = 0.2*min(h^2 Re/4, h/|u|max), red-black SOR with the reference's factor
+(src/main.c:134) to sum|d psi| < 1e-6 from a zero start every step (src/poisson.c). Inputs are
+synthetic: the cavity's own initial condition, nothing is read from disk.
+
+Prints one JSON line. value = Mcell-steps/s = n^2 * steps / (sum of per-step device times),
+each step timed with CUDA events on the library's stream, with L2 flushed (a 256 MB write)
+before every timed step. e2e = the same metric through the C ABI with host buffers: every step
+uploads w, u, v from pinned host memory, runs, and reads w, u, v, psi back, all inside the
+timed region. roofline = the persistent Poisson kernel, algorithmic bytes (24 B per interior
+cell per sweep: read psi and f, write psi) over its CUDA-event duration, against the measured
+HBM copy bandwidth. cpu_baseline = the CPU oracle (a restatement of the reference's own
+algorithm) on this host's cores for one step of the same workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+Under torchrun each rank runs an independent replica (the step does not shard: one cavity per
+GPU); value is the sum over ranks of cells x steps divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fluid-dynamics1_gb300")
+for p in (PKG, os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "Mcell-steps/s at residual 1e-6, mixed/batched vs plain FP64; %HBM peak"
+UNIT = "Mcell-steps/s"
+BYTES_PER_CELL_SWEEP = 24  # FP64: read psi (8) and f (8), write psi (8)
+
+
+def workload(n=1024, re=1000.0, lid=1.0):
+    h = 1.0 / n
+    dt = 0.2 * min(h * h * re / 4.0, h / abs(lid))
+    return dict(n=n, re=re, lid=lid, dt=dt, tol=1e-6, itmax=1000000)
+
+
+def workload_name(w):
+    return (f"lid-driven cavity {w['n']}x{w['n']}, Re {w['re']:g}, lid u={w['lid']:g}, dt={w['dt']:.6g}, "
+            f"red-black SOR (reference beta) to sum|dpsi| < {w['tol']:g} from zero every step")
+
+
+# ------------------------------------------------------------------------------ utilities
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-reduction across torchrun ranks (no-ops for one process)."""
+
+    def __init__(self, ws, device):
+        self.ws = ws
+        self.pg = None
+        if ws > 1:
+            import torch
+            import torch.distributed as td
+
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            td.init_process_group(backend)
+            self.td, self.torch, self.device = td, torch, device
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=f"cuda:{self.device}")
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class L2Flusher:
+    """Writes 256 MB (about twice the 129 MB L2) on the device before each timed step."""
+
+    def __init__(self, device):
+        self.buf = None
+        try:
+            import torch
+
+            if torch.cuda.is_available():
+                self.torch = torch
+                self.buf = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{device}")
+        except Exception:
+            self.buf = None
+
+    def __call__(self):
+        if self.buf is not None:
+            self.buf.fill_(1)
+            self.torch.cuda.synchronize()
+
+    @property
+    def active(self):
+        return self.buf is not None
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic_per_launch():
+    """DRAM bytes (read + write) of one Poisson-kernel launch on this workload, from the
+    committed ncu summary (profiles/poisson_rb_fp64.md, line 'dram_bytes_per_launch: X'), or
+    None. The solve is L2-resident, so this is the compulsory first touch, not per sweep."""
+    path = os.path.join(ROOT, "profiles", "poisson_rb_fp64.md")
+    try:
+        for line in open(path):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+# ------------------------------------------------------------------------------- our arm
+def make_config(cnvpy, w, device, precision=0):
+    return cnvpy.default_config(nx=w["n"], ny=w["n"], Re=w["re"], u4=w["lid"], dt=w["dt"],
+                                poisson_tol=w["tol"], poisson_max_it=w["itmax"], device=device,
+                                precision=precision)
+
+
+def run_device(cnvpy, w, device, steps, warmup, flush, precision=0, clocks=None):
+    """Device-resident run: returns per-step records with CUDA-event times."""
+    cfg = make_config(cnvpy, w, device, precision)
+    recs = []
+    with cnvpy.Cavity(cfg) as cav:
+        for t in range(warmup + steps):
+            flush()
+            if t == warmup and clocks is not None:
+                clocks.start()
+            rc, info = cav.step(1)
+            sweeps, ms, pms = cav.stats()
+            if t >= warmup:
+                recs.append(dict(ms=ms, poisson_ms=pms, sweeps=sweeps, iters=info[0]["iters"]))
+    return recs
+
+
+def run_e2e(cnvpy, w, device, steps, warmup):
+    """Host-buffer run through the C ABI: upload w,u,v, step, read w,u,v,psi, every step."""
+    import numpy as np
+
+    n = w["n"]
+    pinned = False
+    try:
+        import torch
+
+        bufs = [torch.empty((n, n), dtype=torch.float64, pin_memory=True).numpy() for _ in range(4)]
+        pinned = True
+    except Exception:
+        bufs = [np.empty((n, n)) for _ in range(4)]
+    hw, hu, hv, hpsi = bufs
+    cfg = make_config(cnvpy, w, device)
+    with cnvpy.Cavity(cfg) as cav:
+        cw, cu, cv, cpsi = cav.get_fields()
+        hw[...], hu[...], hv[...] = cw, cu, cv
+        lib, h = cav._lib, cav._h
+        ptr = cnvpy._ptr
+        elapsed = 0.0
+        for t in range(warmup + steps):
+            t0 = time.perf_counter()
+            cnvpy.check(lib.cnv_set_fields(h, ptr(hw), ptr(hu), ptr(hv)), "cnv_set_fields")
+            cnvpy.check(lib.cnv_step(h, 1, None), "cnv_step")
+            cnvpy.check(lib.cnv_get_fields(h, ptr(hw), ptr(hu), ptr(hv), ptr(hpsi)), "cnv_get_fields")
+            t1 = time.perf_counter()
+            if t >= warmup:
+                elapsed += t1 - t0
+    return elapsed, pinned
+
+
+def cpu_baseline(w, ncores):
+    """The CPU oracle on this host for one step (step 0) of the workload."""
+    import numpy as np
+    import orc
+
+    orc.build()
+    n = w["n"]
+    p = orc.make_params(n, re=w["re"], dt=w["dt"], u_bc=(0.0, 0.0, 0.0, w["lid"]), tol=w["tol"],
+                        itmax=w["itmax"], threads=ncores, exact_norm=0)
+    W, U, V, PSI = orc.initial_state(n)
+    t0 = time.perf_counter()
+    rc, info = orc.run(p, 1, W, U, V, PSI)
+    t1 = time.perf_counter()
+    return {"value": n * n / (t1 - t0) / 1e6, "unit": UNIT, "cores": ncores, "kind": "port",
+            "sample": f"1 time step (step 0, {info[0]['iters'] + 1} red-black SOR sweeps) of the {n}^2 workload, "
+                      f"oracle/cnv_oracle.c with OpenMP on {ncores} threads, {t1 - t0:.2f} s"}
+
+
+def ours(args):
+    ws, rank, local = dist_env()
+    dist = Dist(ws, local)
+    import cnvpy
+
+    cnvpy.load()
+    w = workload(args.n)
+    flush = L2Flusher(local)
+    clocks = ClockSampler(local) if rank == 0 else None
+    dist.barrier()
+    recs = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=0, clocks=clocks)
+    clk = clocks.stop() if clocks else None
+    dist.barrier()
+    total_ms = sum(r["ms"] for r in recs)
+    total_ms_max = dist.max(total_ms)
+    cells = w["n"] * w["n"]
+    value = ws * cells * args.steps / (total_ms_max * 1e-3) / 1e6
+
+    interior = (w["n"] - 2) ** 2
+    sweeps = sum(r["sweeps"] for r in recs)
+    pms = sum(r["poisson_ms"] for r in recs)
+    achieved = sweeps * interior * BYTES_PER_CELL_SWEEP / (pms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = profiled_traffic_per_launch()
+
+    e2e_s, pinned = run_e2e(cnvpy, w, local, args.steps, args.warmup)
+    e2e_s = dist.max(e2e_s)
+    e2e = {"value": ws * cells * args.steps / e2e_s / 1e6, "unit": UNIT,
+           "h2d_bytes_per_step": 3 * cells * 8, "d2h_bytes_per_step": 4 * cells * 8,
+           "host_buffers": "pinned" if pinned else "pageable"}
+
+    forms = {}
+    if not args.skip_forms:
+        fma = run_device(cnvpy, w, local, max(2, args.steps // 4), 1, flush, precision=1)
+        f_ms = sum(r["ms"] for r in fma)
+        forms["fp64_fma"] = {"value": cells * len(fma) / (f_ms * 1e-3) / 1e6, "unit": UNIT,
+                             "steps": len(fma), "sweeps_per_step": sum(r["sweeps"] for r in fma) / len(fma)}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        cpu = cpu_baseline(w, os.cpu_count() or 1)
+
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms_max / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(w), "grid": w["n"], "precision": "fp64 (reference rounding)",
+                   "l2": "flushed before every timed step (256 MB device write)" if flush.active else "not flushed",
+                   "parallelism": f"replicas x{ws}", "sweeps_per_step": round(sweeps / len(recs), 1),
+                   "first_step": args.warmup},
+        "Mcell_sweeps_per_s": round(interior * sweeps / (pms * 1e-3) / 1e6, 2),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "k_poisson (persistent red-black SOR, one launch per step)"},
+        "e2e": e2e,
+        "gpu_launches": 5 * args.steps,
+        "clocks": clk,
+        "forms": forms,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+# ------------------------------------------------------------------------- reference arm
+def reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return  # the reference is CPU code: rank 0 alone runs it
+    import numpy as np
+    import orc
+
+    orc.build()
+    w = workload(args.n)
+    n = w["n"]
+    cores = os.cpu_count() or 1
+    p = orc.make_params(n, re=w["re"], dt=w["dt"], u_bc=(0.0, 0.0, 0.0, w["lid"]), tol=w["tol"],
+                        itmax=w["itmax"], threads=cores, exact_norm=0)
+    W, U, V, PSI = orc.initial_state(n)
+    for _ in range(args.warmup):
+        orc.run(p, 1, W, U, V, PSI)
+    t0 = time.perf_counter()
+    rc, info = orc.run(p, args.steps, W, U, V, PSI)
+    t1 = time.perf_counter()
+    value = n * n * args.steps / (t1 - t0) / 1e6
+    # The reference's own dense operators need 4*(n^2)^2*8 bytes (35 TB at 1024^2), so its CPU path
+    # at this size is the banded restatement (bitwise-equal to it where both run).
+    kind = "port"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round((t1 - t0) * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(w), "grid": n,
+                   "sweeps_per_step": round(sum(s["iters"] + 1 for s in info) / len(info), 1)},
+        "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"steps {args.warmup}..{args.warmup + args.steps - 1} of the {n}^2 workload, "
+                                   f"oracle/cnv_oracle.c (restatement of the reference's CPU path, red-black "
+                                   f"SOR) with OpenMP on {cores} threads"},
+        "e2e": {"value": round(value, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1024, help=argparse.SUPPRESS)
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
+    ap.add_argument("--skip-forms", action="store_true", help="omit the extra precision/batch forms")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)  # at least 3 untimed warm-up steps
+    if args.impl == "reference":
+        reference(args)
+    else:
+        ours(args)
+
+
+if __name__ == "__main__":
+    main()

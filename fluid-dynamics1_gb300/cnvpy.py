@@ -1,0 +1,225 @@
+"""Thin ctypes binding of libcnv (include/cnv.h) for tests, the benchmark and Python callers.
+
+This mirrors the C ABI one to one; the GPU work all happens inside libcnv.so. If the library is
+missing or fails to load, every entry point raises: there is no Python or CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcnv.so")
+
+CNV_OK, CNV_NOT_CONVERGED, CNV_NONFINITE, CNV_BAD_ARG = 0, 1, 2, 3
+CNV_CUDA_ERROR, CNV_TIMEOUT, CNV_NO_DEVICE, CNV_IO_ERROR = 4, 5, 6, 7
+STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "NONFINITE", 3: "BAD_ARG", 4: "CUDA_ERROR",
+                5: "TIMEOUT", 6: "NO_DEVICE", 7: "IO_ERROR"}
+POISSON_GS, POISSON_SOR, POISSON_JACOBI = 1, 2, 3
+PREC_FP64, PREC_FP64_FMA, PREC_MIXED = 0, 1, 2
+INIT_REFERENCE, INIT_NOISE = 0, 1
+
+
+class CnvError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("Re", C.c_double), ("Lx", C.c_int), ("Ly", C.c_int), ("nx", C.c_int), ("ny", C.c_int),
+        ("dt", C.c_double), ("tf", C.c_double), ("max_co", C.c_double), ("order", C.c_int),
+        ("poisson_max_it", C.c_int), ("poisson_tol", C.c_double), ("output_interval", C.c_int),
+        ("poisson_type", C.c_int), ("openmp_enabled", C.c_int),
+        ("ui", C.c_double), ("vi", C.c_double),
+        ("u1", C.c_double), ("u2", C.c_double), ("u3", C.c_double), ("u4", C.c_double),
+        ("v1", C.c_double), ("v2", C.c_double), ("v3", C.c_double), ("v4", C.c_double),
+        ("sor_omega", C.c_double), ("nsteps", C.c_int), ("precision", C.c_int),
+        ("mixed_rtol", C.c_double), ("init_field", C.c_int), ("seed", C.c_ulonglong),
+        ("init_sigma", C.c_double), ("init_smooth_passes", C.c_int), ("device", C.c_int),
+        ("reserved", C.c_int * 8),
+    ]
+
+
+class StepInfo(C.Structure):
+    _fields_ = [("iters", C.c_int), ("status", C.c_int), ("err", C.c_double),
+                ("cont_max", C.c_double), ("cont_min", C.c_double)]
+
+
+_dp = C.POINTER(C.c_double)
+_lib = None
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "cnv_config_default": (C.c_int, [C.POINTER(Config)]),
+    "cnv_config_load": (C.c_int, [C.c_char_p, C.POINTER(Config)]),
+    "cnv_config_set": (C.c_int, [C.POINTER(Config), C.c_char_p, C.c_char_p]),
+    "cnv_config_steps": (C.c_int, [C.POINTER(Config)]),
+    "cnv_create": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
+    "cnv_destroy": (None, [C.c_void_p]),
+    "cnv_reset": (C.c_int, [C.c_void_p]),
+    "cnv_grid_size": (C.c_int, [C.c_void_p]),
+    "cnv_set_fields": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "cnv_get_fields": (C.c_int, [C.c_void_p, _dp, _dp, _dp, _dp]),
+    "cnv_set_fields_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cnv_get_fields_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "cnv_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepInfo)]),
+    "cnv_step_async": (C.c_int, [C.c_void_p, C.c_int]),
+    "cnv_sync": (C.c_int, [C.c_void_p, C.POINTER(StepInfo), C.c_int]),
+    "cnv_step_rows": (C.c_int, [C.c_void_p, C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp),
+                                C.POINTER(_dp), C.POINTER(StepInfo)]),
+    "cnv_poisson": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int), _dp]),
+    "cnv_poisson_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), _dp]),
+    "cnv_last_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _dp, _dp]),
+    "cnv_last_error": (C.c_char_p, []),
+    "cnv_version": (C.c_char_p, []),
+}
+
+
+def load(path: str | None = None):
+    """Load libcnv.so (building it first if it is missing). Raises if it cannot be loaded."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        import importlib.util
+
+        spec = importlib.util.spec_from_file_location("cnv_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def last_error() -> str:
+    return load().cnv_last_error().decode(errors="replace")
+
+
+def check(status: int, what: str = "") -> None:
+    if status != CNV_OK:
+        raise CnvError(status, f"{what}: {last_error()}")
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"], "fields must be C-contiguous float64"
+    return a.ctypes.data_as(_dp)
+
+
+def default_config(**overrides) -> Config:
+    cfg = Config()
+    check(load().cnv_config_default(C.byref(cfg)), "cnv_config_default")
+    for k, v in overrides.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+def load_config(path: str) -> tuple[int, Config]:
+    cfg = Config()
+    rc = load().cnv_config_load(path.encode(), C.byref(cfg))
+    return rc, cfg
+
+
+def config_steps(cfg: Config) -> int:
+    return load().cnv_config_steps(C.byref(cfg))
+
+
+class Cavity:
+    """One device-resident cavity (cnv_state)."""
+
+    def __init__(self, cfg: Config):
+        self._lib = load()
+        self.cfg = cfg
+        h = C.c_void_p()
+        check(self._lib.cnv_create(C.byref(cfg), C.byref(h)), "cnv_create")
+        self._h = h
+        self.n = cfg.nx
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.cnv_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def reset(self):
+        check(self._lib.cnv_reset(self._h), "cnv_reset")
+
+    def set_fields(self, w=None, u=None, v=None) -> int:
+        return self._lib.cnv_set_fields(self._h, _ptr(w), _ptr(u), _ptr(v))
+
+    def get_fields(self):
+        n = self.n
+        w, u, v, psi = (np.empty((n, n)) for _ in range(4))
+        check(self._lib.cnv_get_fields(self._h, _ptr(w), _ptr(u), _ptr(v), _ptr(psi)), "cnv_get_fields")
+        return w, u, v, psi
+
+    def step(self, nsteps: int = 1, raise_on_error: bool = True):
+        """Advance nsteps; returns (status, list of per-step dicts)."""
+        info = (StepInfo * max(nsteps, 1))()
+        rc = self._lib.cnv_step(self._h, nsteps, info)
+        if rc != CNV_OK and raise_on_error:
+            raise CnvError(rc, last_error())
+        return rc, [dict(iters=info[t].iters, status=info[t].status, err=info[t].err,
+                         cont_max=info[t].cont_max, cont_min=info[t].cont_min) for t in range(nsteps)]
+
+    def step_async(self, nsteps: int) -> None:
+        check(self._lib.cnv_step_async(self._h, nsteps), "cnv_step_async")
+
+    def sync(self, nsteps: int = 0):
+        info = (StepInfo * max(nsteps, 1))()
+        rc = self._lib.cnv_sync(self._h, info, nsteps)
+        return rc, [dict(iters=info[t].iters, status=info[t].status, err=info[t].err,
+                         cont_max=info[t].cont_max, cont_min=info[t].cont_min) for t in range(nsteps)]
+
+    def step_rows(self, w, u, v, psi):
+        """cnv_step_rows on row-pointer arrays built from the given (n, n) numpy fields."""
+        rows = lambda a: (_dp * self.n)(*[a[i].ctypes.data_as(_dp) for i in range(self.n)])
+        info = StepInfo()
+        rc = self._lib.cnv_step_rows(self._h, rows(w), rows(u), rows(v), rows(psi), C.byref(info))
+        return rc, dict(iters=info.iters, status=info.status, err=info.err, cont_max=info.cont_max,
+                        cont_min=info.cont_min)
+
+    def poisson(self, f):
+        psi = np.empty_like(f)
+        it, err = C.c_int(0), C.c_double(0.0)
+        rc = self._lib.cnv_poisson(self._h, _ptr(np.ascontiguousarray(f)), _ptr(psi), C.byref(it), C.byref(err))
+        return rc, psi, it.value, err.value
+
+    def stats(self):
+        """(sweeps, ms of the last call, ms of the last Poisson kernel) -- CUDA-event times."""
+        sw, ms, pms = C.c_longlong(0), C.c_double(0), C.c_double(0)
+        check(self._lib.cnv_last_stats(self._h, C.byref(sw), C.byref(ms), C.byref(pms)), "cnv_last_stats")
+        return sw.value, ms.value, pms.value
+
+    # device-pointer variants (torch tensors or any CUDA allocation); pointers are ints
+    def set_fields_device(self, w=0, u=0, v=0) -> int:
+        return self._lib.cnv_set_fields_device(self._h, w or None, u or None, v or None)
+
+    def get_fields_device(self, w=0, u=0, v=0, psi=0) -> int:
+        return self._lib.cnv_get_fields_device(self._h, w or None, u or None, v or None, psi or None)

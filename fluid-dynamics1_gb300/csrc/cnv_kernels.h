@@ -1,0 +1,63 @@
+// cnv_kernels.h -- launchers of libcnv's CUDA kernels (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "cnv_internal.h"
+
+namespace cnv {
+
+// Buffers and scalars of one time step. Pointers are device pointers.
+struct StepArgs {
+    int n;
+    int pitch;                 // split-layout row pitch in doubles
+    const double* w_in;        // vorticity at step start (wall values written in place)
+    double* w_wall;            // == w_in, writable view for the wall pass
+    double* w_out;             // vorticity after the Euler update
+    double* u;                 // velocities, row-major
+    double* v;
+    double* psi;               // streamfunction, row-major (output copy)
+    double* sor[2];            // psi, red/black split layout
+    double* rhs[2];            // Poisson right-hand side, split layout
+    const FdBands* bands;      // device copy of the operator bands
+    BoundaryValues bc;
+    double inv_re;             // 1. / Re as src/fluiddyn.c:98 evaluates it
+    double dt;
+    double c4;                 // dx*dx*dy*dy (src/poisson.c:247 evaluates it left to right)
+    int rhs_mode;              // 0: rhs = c4 * f; 1: rhs = (c4 * f) / den (FMA form)
+    double rhs_den;
+    double rhs_rden;
+    int rhs_den_pow2;
+    Ctrl* ctrl;
+    double* cont_partials;     // 2 * cont_blocks doubles
+    int cont_blocks;
+};
+
+cudaError_t launch_wall(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_transport(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_velocity(const StepArgs& a, cudaStream_t s);
+cudaError_t launch_continuity(const StepArgs& a, cudaStream_t s);
+// Copy a row-major field into the split layout and back (parity tests of the solver alone).
+// to_split applies the same right-hand-side scaling as the transport pass (a.c4, a.rhs_mode).
+cudaError_t launch_to_split(const double* f, double* r, double* b, const StepArgs& a, cudaStream_t s);
+cudaError_t launch_from_split(const double* r, const double* b, double* f, int n, int pitch,
+                              cudaStream_t s);
+// Scan n*n doubles for NaN/Inf; *flag (device int) is set to 1 when one is found.
+cudaError_t launch_nonfinite_scan(const double* x, long long count, int* flag, cudaStream_t s);
+
+// Persistent red-black Poisson solver (cooperative launch). sor/rhs are split-layout arrays;
+// alt is a second split pair used by Jacobi. grid = number of co-resident blocks.
+struct PoissonLaunch {
+    PoissonParams p;
+    double* sor[2];
+    double* alt[2];
+    const double* rhs[2];
+    Ctrl* ctrl;
+    double* partials;          // 2 * grid doubles
+    int grid;
+};
+cudaError_t launch_poisson(const PoissonLaunch& L, cudaStream_t s);
+int poisson_threads();
+const void* poisson_kernel_ptr(Arith a, int kind);
+
+}  // namespace cnv

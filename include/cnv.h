@@ -1,0 +1,173 @@
+/*
+ * cnv.h -- C ABI of libcnv, the GB300 (sm_103a) implementation of cnavier's explicit
+ * vorticity-streamfunction time step (SorinBetisor/fluid-dynamics1).
+ *
+ * The library replaces the body of cnavier's time loop, src/main.c:283-395:
+ *   velocity BCs (:283-296) -> wall vorticity (:298-320) -> vorticity derivatives and the
+ *   Euler update (:323-344, src/fluiddyn.c:71-102) -> Poisson solve for psi with f = -w
+ *   (:347-363, src/poisson.c) -> u = DY psi, v = -DX psi (:366-383) -> continuity
+ *   diagnostic (:387-408).
+ * All state stays on the GPU between steps. Every entry point returns a cnv_status and never
+ * exits the process (the reference calls exit(1) on the failures listed below).
+ *
+ * Conventions: fields are n x n doubles, row-major (index i*n + j), i is the reference's first
+ * index (the lid is row i = n-1), exactly the flattening of src/linearalg.c:373-408. Host
+ * pointers are plain host memory; *_device entry points take device pointers. One state is
+ * used by one host thread at a time; each state owns one CUDA stream.
+ *
+ * The reference-shaped entry points (euler, poisson_SOR, ... with mtrx arguments) live in
+ * cnv_compat.h.
+ */
+#ifndef CNV_H
+#define CNV_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CNV_ABI_VERSION 1
+
+typedef enum cnv_status {
+    CNV_OK = 0,
+    CNV_NOT_CONVERGED = 1, /* Poisson solve reached poisson_max_it; src/poisson.c:168-172 exits */
+    CNV_NONFINITE = 2,     /* NaN or Inf in an input field or in the stop norm */
+    CNV_BAD_ARG = 3,       /* invalid size, order, solver type or pointer */
+    CNV_CUDA_ERROR = 4,    /* a CUDA runtime call failed; see cnv_last_error() */
+    CNV_TIMEOUT = 5,       /* a bounded on-device wait gave up */
+    CNV_NO_DEVICE = 6,     /* no usable sm_103 device */
+    CNV_IO_ERROR = 7       /* config or output file could not be read or written */
+} cnv_status;
+
+/* Poisson solver selection (config key poisson_type, src/main.c:349-361). */
+enum {
+    CNV_POISSON_GS = 1,     /* "no relaxation" (src/poisson.c:62-109), run as red-black GS */
+    CNV_POISSON_SOR = 2,    /* SOR (src/poisson.c:111-173), red-black ordering */
+    CNV_POISSON_JACOBI = 3  /* true Jacobi sweeps (extension; src/cuda_kernels.cu:229-246) */
+};
+
+/* Arithmetic of the Poisson sweeps (extension key "precision"). */
+enum {
+    CNV_PREC_FP64 = 0,      /* FP64, the reference's operation order and rounding (default) */
+    CNV_PREC_FP64_FMA = 1,  /* FP64, fused multiply-add form of the same update */
+    CNV_PREC_MIXED = 2      /* FP32 sweeps inside FP64 defect correction */
+};
+
+/* Initial vorticity (extension key "init_field"). */
+enum {
+    CNV_INIT_REFERENCE = 0, /* w = psi = 0, interior u = ui, v = vi (src/main.c:178-221) */
+    CNV_INIT_NOISE = 1      /* seeded Gaussian noise smoothed by Jacobi averaging passes */
+};
+
+/*
+ * Configuration: the reference's Config (include/config.h:4-36), same names, types and
+ * meaning, followed by optional extension keys whose defaults reproduce the reference.
+ */
+typedef struct cnv_config {
+    /* --- include/config.h:4-36 --- */
+    double Re;
+    int Lx;
+    int Ly;
+    int nx;
+    int ny;
+    double dt;
+    double tf;
+    double max_co;
+    int order;
+    int poisson_max_it;
+    double poisson_tol;
+    int output_interval;
+    int poisson_type;
+    int openmp_enabled;  /* kept for file compatibility; the GPU always sweeps red-black */
+    double ui, vi;
+    double u1, u2, u3, u4;
+    double v1, v2, v3, v4;
+    /* --- extensions --- */
+    double sor_omega;        /* SOR factor; <= 0 selects the reference formula, src/main.c:134 */
+    int nsteps;              /* steps to run; <= 0 selects (int)(tf/dt - 1) + 1, src/main.c:162 */
+    int precision;           /* CNV_PREC_* */
+    double mixed_rtol;       /* CNV_PREC_MIXED: stop when ||f - A psi||_2 / ||f||_2 <= mixed_rtol;
+                                <= 0 keeps the reference stop rule (sum |d psi| < poisson_tol) */
+    int init_field;          /* CNV_INIT_* */
+    unsigned long long seed; /* CNV_INIT_NOISE generator seed (splitmix64) */
+    double init_sigma;       /* CNV_INIT_NOISE standard deviation */
+    int init_smooth_passes;  /* CNV_INIT_NOISE Jacobi averaging passes */
+    int device;              /* CUDA device ordinal */
+    int reserved[8];
+} cnv_config;
+
+/* Per-step record: the values the reference logs (src/poisson.c:275, src/main.c:407-408). */
+typedef struct cnv_step_info {
+    int iters;        /* k of the sweep that met the tolerance (0-based), as logged */
+    int status;       /* cnv_status of this step */
+    double err;       /* stop norm of that sweep */
+    double cont_max;  /* maxel(DX u + DY v) */
+    double cont_min;  /* minel(DX u + DY v) */
+} cnv_step_info;
+
+typedef struct cnv_state cnv_state;
+
+/* load_default_config(), src/config.c:47-87, plus extension defaults. */
+int cnv_config_default(cnv_config *cfg);
+/* load_config_from_file(), src/config.c:106-214: same key = value format, comments, trimming
+ * and warnings; a missing file keeps the defaults and returns CNV_IO_ERROR (the reference
+ * prints a message and continues with the defaults). */
+int cnv_config_load(const char *path, cnv_config *cfg);
+/* Apply one key/value pair as the parser would (returns CNV_BAD_ARG for an unknown key). */
+int cnv_config_set(cnv_config *cfg, const char *key, const char *value);
+/* Steps the reference would run: it_max + 1 with it_max = (int)(tf/dt - 1) (src/main.c:162),
+ * or cfg->nsteps when positive. */
+int cnv_config_steps(const cnv_config *cfg);
+
+/* Create the device state for cfg (nx == ny required, as the reference's Kronecker operators
+ * are; src/linearalg.c:367). The fields start as src/main.c:178-221 sets them (or as
+ * init_field selects). */
+int cnv_create(const cnv_config *cfg, cnv_state **out);
+void cnv_destroy(cnv_state *s);
+/* Back to the initial condition. */
+int cnv_reset(cnv_state *s);
+int cnv_grid_size(const cnv_state *s);
+
+/* Copy fields in or out (n*n doubles each, row-major). NULL pointers are skipped.
+ * cnv_set_fields returns CNV_NONFINITE (and changes nothing) if an input holds NaN or Inf. */
+int cnv_set_fields(cnv_state *s, const double *w, const double *u, const double *v);
+int cnv_get_fields(cnv_state *s, double *w, double *u, double *v, double *psi);
+int cnv_set_fields_device(cnv_state *s, const double *w, const double *u, const double *v);
+int cnv_get_fields_device(cnv_state *s, double *w, double *u, double *v, double *psi);
+
+/* Advance nsteps time steps (src/main.c:283-395 each). info may be NULL or hold nsteps
+ * records. Stops at the first step whose solve does not converge or goes non-finite and
+ * returns that step's status. Synchronises the state's stream before returning. */
+int cnv_step(cnv_state *s, int nsteps, cnv_step_info *info);
+/* Same, but only enqueues the work on the state's stream; cnv_sync() waits and fills info. */
+int cnv_step_async(cnv_state *s, int nsteps);
+int cnv_sync(cnv_state *s, cnv_step_info *info, int ninfo);
+
+/* Drop-in replacement of the whole loop body for a caller that keeps its fields in the
+ * reference's row-pointer layout (mtrx.M, src/linearalg.c:53-82): uploads w, u, v, runs one
+ * step and writes w, u, v and psi back, as src/main.c:283-395 leaves them. */
+int cnv_step_rows(cnv_state *s, double **w, double **u, double **v, double **psi,
+                  cnv_step_info *info);
+
+/* Poisson solve alone, poisson_SOR() / poisson() semantics (src/poisson.c:111-173, :62-109):
+ * psi = 0 start, Dirichlet psi = 0 on the edge, stop at sum |psi_k+1 - psi_k| < tol.
+ * f and psi are host arrays of n*n doubles; uses the state's grid, spacing and solver
+ * settings. iters/err may be NULL. */
+int cnv_poisson(cnv_state *s, const double *f, double *psi, int *iters, double *err);
+int cnv_poisson_device(cnv_state *s, const double *f, double *psi, int *iters, double *err);
+
+/* Statistics of the last cnv_step/cnv_poisson call: total Poisson sweeps, device time of the
+ * whole call (ms, CUDA events on the state's stream) and device time of the Poisson kernel of
+ * the last step or solve it ran (ms). Any pointer may be NULL. */
+int cnv_last_stats(cnv_state *s, long long *sweeps, double *ms, double *poisson_ms);
+
+/* Human-readable text for the last failing call on this thread. */
+const char *cnv_last_error(void);
+/* Library version and the device it was built for. */
+const char *cnv_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CNV_H */

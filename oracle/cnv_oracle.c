@@ -318,7 +318,7 @@ int orc_run(const orc_params *p, int nsteps, double *w, double *u, double *v, do
     double *d1x, *d1y, *d2x, *d2y;
     double *a, *b, *c, *d, *f;
 
-    if (n < 5 || nsteps < 0) return ORC_BAD_ARG;
+    if (n < 4 || nsteps < 0) return ORC_BAD_ARG;
 #ifdef _OPENMP
     if (p->threads > 0) omp_set_num_threads(p->threads);
 #endif

@@ -1,0 +1,183 @@
+"""CUDA path vs the CPU oracle, through the C ABI of libcnv.
+
+Tolerances: the FP64 path with reference arithmetic (precision = fp64) must match the oracle
+bit for bit on every field (same operation order, round-to-nearest, no FMA contraction);
+iteration counts must be equal; the stop norm is summed in a different order on the GPU, so it
+is compared to 1e-12 relative. The FMA form must agree to 1e-10 normwise relative
+(max|a-b| / max|b|) per field, inside the benchmark spec's bound of 1e-8 relative.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "logs_kat.json")
+REL_ERR_TOL = 1e-12       # stop norm, GPU vs oracle (different summation order)
+FMA_FIELD_TOL = 1e-10     # FMA form, normwise relative per field
+
+
+def make_cfg(cnv, n, **kw):
+    base = dict(nx=n, ny=n, Re=1000.0, dt=0.005, poisson_tol=1e-3, poisson_max_it=10000, order=6)
+    base.update(kw)
+    return cnv.default_config(**base)
+
+
+def oracle_params(orc, cfg, ordering=1):
+    return orc.make_params(cfg.nx, order=cfg.order, Lx=cfg.Lx, Ly=cfg.Ly, re=cfg.Re, dt=cfg.dt,
+                           u_bc=(cfg.u1, cfg.u2, cfg.u3, cfg.u4), v_bc=(cfg.v1, cfg.v2, cfg.v3, cfg.v4),
+                           poisson_type=cfg.poisson_type, ordering=ordering,
+                           beta=(cfg.sor_omega if cfg.sor_omega > 0 else None), itmax=cfg.poisson_max_it,
+                           tol=cfg.poisson_tol, threads=0, exact_norm=0)
+
+
+def bitwise(a, b):
+    return np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64))
+
+
+def run_both(cnv, orc, cfg, nsteps):
+    with cnv.Cavity(cfg) as cav:
+        rc, gsteps = cav.step(nsteps)
+        gw, gu, gv, gpsi = cav.get_fields()
+    p = oracle_params(orc, cfg)
+    w, u, v, psi = orc.initial_state(cfg.nx, cfg.ui, cfg.vi)
+    orc_rc, osteps = orc.run(p, nsteps, w, u, v, psi)
+    assert rc == 0 and orc_rc == 0
+    return (gw, gu, gv, gpsi), gsteps, (w, u, v, psi), osteps
+
+
+@pytest.mark.parametrize("n,order", [(7, 6), (8, 6), (16, 6), (33, 6), (64, 6), (32, 4), (32, 2), (5, 6), (4, 4)])
+def test_step_bitwise_equals_oracle(cnv, orc, n, order):
+    cfg = make_cfg(cnv, n, order=order)
+    g, gs, o, os_ = run_both(cnv, orc, cfg, 6)
+    for name, a, b in zip("w u v psi".split(), g, o):
+        assert bitwise(a, b), f"{name} differs: max abs {np.max(np.abs(a - b))}"
+    for a, b in zip(gs, os_):
+        assert a["iters"] == b["iters"]
+        assert abs(a["err"] - b["err"]) <= REL_ERR_TOL * abs(b["err"])
+        assert bitwise(a["cont_max"], b["cont_max"]) and bitwise(a["cont_min"], b["cont_min"])
+
+
+def test_step_all_boundary_values_and_rectangular_spacing(cnv, orc):
+    cfg = make_cfg(cnv, 24, Lx=2, Ly=1, Re=400.0, dt=0.001, poisson_tol=1e-6, u1=0.1, u2=-0.2, u3=0.3,
+                   u4=1.0, v1=0.05, v2=-0.05, v3=0.02, v4=-0.03, ui=0.01, vi=-0.02)
+    g, gs, o, os_ = run_both(cnv, orc, cfg, 4)
+    for a, b in zip(g, o):
+        assert bitwise(a, b)
+
+
+@pytest.mark.parametrize("run", ["testRunOMP", "testRunOMPHIGHRES"])
+def test_gpu_reproduces_shipped_redblack_logs(cnv, run):
+    """The reference's own red-black run logs, every logged step, printed digits."""
+    spec = json.load(open(GOLDEN))[run]
+    n = spec["n"]
+    cfg = make_cfg(cnv, n, Re=spec["re"], dt=spec["dt"], poisson_tol=spec["tol"], poisson_max_it=spec["itmax"])
+    steps = spec["steps"]
+    with cnv.Cavity(cfg) as cav:
+        rc, got = cav.step(len(steps))
+    assert rc == 0
+    for t, (a, b) in enumerate(zip(got, steps)):
+        assert a["iters"] == b["iters"], f"step {t}"
+        assert "%E" % a["err"] == b["err"], f"step {t}"
+        assert "%E" % a["cont_max"] == b["cont_max"] and "%E" % a["cont_min"] == b["cont_min"], f"step {t}"
+
+
+def test_config1_64_re100_sor15(cnv, orc):
+    """The CPU workload: 64^2, Re 100, dt 1e-3, SOR beta 1.5, tol 1e-6 (first 20 of its 1000 steps)."""
+    cfg = make_cfg(cnv, 64, Re=100.0, dt=1e-3, poisson_tol=1e-6, sor_omega=1.5)
+    g, gs, o, os_ = run_both(cnv, orc, cfg, 20)
+    for a, b in zip(g, o):
+        assert bitwise(a, b)
+    assert [s["iters"] for s in gs] == [s["iters"] for s in os_]
+
+
+@pytest.mark.parametrize("ptype", [1, 2, 3])
+@pytest.mark.parametrize("n", [16, 37, 96])
+def test_poisson_alone_matches_oracle(cnv, orc, ptype, n):
+    rng = np.random.default_rng(n * 10 + ptype)
+    f = rng.standard_normal((n, n))
+    cfg = make_cfg(cnv, n, poisson_type=ptype, poisson_tol=1e-9, poisson_max_it=200000)
+    with cnv.Cavity(cfg) as cav:
+        rc, psi, it, err = cav.poisson(f)
+    p = oracle_params(orc, cfg)
+    opsi, oit, oerr, orc_rc = orc.poisson(p, f)
+    assert rc == 0 and orc_rc == 0
+    assert it == oit
+    assert bitwise(psi, opsi)
+    assert abs(err - oerr) <= REL_ERR_TOL * oerr
+
+
+@pytest.mark.parametrize("n", [64, 100, 128])
+def test_fma_form_within_tolerance(cnv, orc, n):
+    cfg = make_cfg(cnv, n, precision=1, poisson_tol=1e-8)
+    g, gs, o, os_ = run_both(cnv, orc, cfg, 5)
+    for name, a, b in zip("w u v psi".split(), g, o):
+        scale = max(np.max(np.abs(b)), 1e-300)
+        assert np.max(np.abs(a - b)) / scale <= FMA_FIELD_TOL, name
+    for a, b in zip(gs, os_):
+        assert abs(a["iters"] - b["iters"]) <= 1
+
+
+def test_1024_single_step_matches_oracle(cnv, orc):
+    """The benchmark workload's grid (1024^2, Re 1000, dt by the stability rule, tol 1e-6), step 0."""
+    n = 1024
+    h = 1.0 / n
+    dt = 0.2 * min(h * h * 1000.0 / 4, h / 1.0)
+    cfg = make_cfg(cnv, n, Re=1000.0, dt=dt, poisson_tol=1e-6, poisson_max_it=100000)
+    g, gs, o, os_ = run_both(cnv, orc, cfg, 1)
+    for name, a, b in zip("w u v psi".split(), g, o):
+        assert bitwise(a, b), name
+    assert gs[0]["iters"] == os_[0]["iters"]
+
+
+# ------------------------------------------------------------------------- failure paths
+def test_itmax_reports_not_converged_and_stops(cnv):
+    cfg = make_cfg(cnv, 32, poisson_max_it=2, poisson_tol=1e-12)
+    with cnv.Cavity(cfg) as cav:
+        rc, steps = cav.step(3, raise_on_error=False)
+    assert rc == cnv.CNV_NOT_CONVERGED
+    assert steps[0]["status"] == cnv.CNV_NOT_CONVERGED and steps[0]["iters"] == 2
+
+
+def test_nonfinite_input_rejected(cnv):
+    cfg = make_cfg(cnv, 16)
+    with cnv.Cavity(cfg) as cav:
+        w = np.zeros((16, 16))
+        w[3, 4] = np.nan
+        assert cav.set_fields(w=w) == cnv.CNV_NONFINITE
+        w[3, 4] = np.inf
+        assert cav.set_fields(w=w) == cnv.CNV_NONFINITE
+        rc, steps = cav.step(1)
+        assert rc == 0
+
+
+def test_step_rows_matches_step(cnv):
+    n = 20
+    cfg = make_cfg(cnv, n)
+    with cnv.Cavity(cfg) as a:
+        a.step(3)
+        ref = a.get_fields()
+    with cnv.Cavity(cfg) as b:
+        w, u, v, psi = b.get_fields()
+        for _ in range(3):
+            rc, info = b.step_rows(w, u, v, psi)
+            assert rc == 0
+    for x, y in zip(ref, (w, u, v, psi)):
+        assert bitwise(x, y)
+
+
+def test_reset_and_repeat_is_deterministic(cnv):
+    cfg = make_cfg(cnv, 48)
+    with cnv.Cavity(cfg) as cav:
+        _, s1 = cav.step(4)
+        f1 = cav.get_fields()
+        cav.reset()
+        _, s2 = cav.step(4)
+        f2 = cav.get_fields()
+    assert s1 == s2
+    for a, b in zip(f1, f2):
+        assert bitwise(a, b)
