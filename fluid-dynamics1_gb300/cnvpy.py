@@ -74,6 +74,9 @@ _SIGS = {
     "cnv_poisson": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int), _dp]),
     "cnv_poisson_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), _dp]),
     "cnv_last_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _dp, _dp]),
+    "cnv_poisson_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
+                                      C.c_int, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), _dp,
+                                      C.c_void_p]),
     "cnv_last_error": (C.c_char_p, []),
     "cnv_version": (C.c_char_p, []),
 }

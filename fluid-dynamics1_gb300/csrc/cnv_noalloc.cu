@@ -1,0 +1,177 @@
+// cnv_noalloc.cu -- a Poisson solve that allocates no device memory.
+//
+// Who needs this: some callers may not allocate GPU memory once they are running. Examples are
+// a host application whose memory pool already owns the whole device, and a real-time loop
+// that forbids cudaMalloc/cudaFree after start-up. cudaFree synchronises the whole device and
+// both calls take unbounded time. Such a caller cannot create a cnv_state, because
+// cnv_create allocates the working buffers. cnv_poisson_noalloc takes only the caller's input
+// and output arrays and keeps every intermediate array (the red/black copies of psi and of the
+// right-hand side, the per-block partial sums, the control block) in the file-scope array
+// g_scratch below. The array is placed in device memory when the library's module is loaded,
+// and every GPU that loads the library keeps it until the process exits.
+//
+// Limits and sharing rules:
+//   - grids up to kMaxN x kMaxN (512 x 512); larger n is rejected with CNV_BAD_ARG;
+//   - Gauss-Seidel and SOR only (poisson_type 1 or 2); Jacobi would need a second psi copy;
+//   - all calls on a device share g_scratch, which keeps the previous call's contents. Each
+//     call clears what must start at zero (psi and the control block), so back-to-back calls
+//     are independent, but two calls whose GPU work overlaps (different streams or host
+//     threads at the same time) race on the same memory and give wrong results.
+//   - the first call on each device looks up the device address of g_scratch with
+//     cudaGetSymbolAddress (with that device current) and caches it; make that first call
+//     outside any stream capture.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "cnv_kernels.h"
+
+namespace cnv {
+namespace {
+
+constexpr int kMaxN = 512;
+constexpr int kMaxPitch = ((kMaxN + 1) / 2 + 31) / 32 * 32;  // 256 doubles per split row
+constexpr size_t kSplitBytes = (size_t)kMaxN * kMaxPitch * sizeof(double);
+constexpr int kMaxGrid = 1024;                               // Poisson blocks
+constexpr size_t kCtrlBytes = 256;
+constexpr size_t kPartialBytes = 2 * kMaxGrid * sizeof(double);
+// control block | partials | psi red | psi black | rhs red | rhs black
+constexpr size_t kScratchBytes = kCtrlBytes + kPartialBytes + 4 * kSplitBytes;
+static_assert(sizeof(Ctrl) <= kCtrlBytes, "control block does not fit its slot");
+
+static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mutex;
+unsigned char* g_scratch_addr[kMaxDevices] = {};
+
+// This entry point has no state to hold an error string, so it reports why it failed on stderr
+// and returns the status code.
+int error(int status, const char* msg) {
+    std::fprintf(stderr, "cnv_poisson_noalloc: %s\n", msg);
+    return status;
+}
+
+}  // namespace
+}  // namespace cnv
+
+using namespace cnv;
+
+extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double dx, double dy,
+                                   int poisson_type, int precision, double beta, int itmax,
+                                   double tol, int* iters, double* err, void* stream_handle) {
+    if (!f || !psi) return error(CNV_BAD_ARG, "null input or output pointer");
+    if (n < 3 || n > kMaxN)
+        return error(CNV_BAD_ARG, "grid size n must be between 3 and 512 (the size of the built-in scratch array)");
+    if (poisson_type != CNV_POISSON_GS && poisson_type != CNV_POISSON_SOR)
+        return error(CNV_BAD_ARG, "poisson_type must be 1 (Gauss-Seidel) or 2 (SOR)");
+    if (precision != CNV_PREC_FP64 && precision != CNV_PREC_FP64_FMA)
+        return error(CNV_BAD_ARG, "precision must be fp64 (0) or fp64_fma (1)");
+    if (!(dx > 0) || !(dy > 0) || itmax < 1 || !(tol >= 0))
+        return error(CNV_BAD_ARG, "invalid dx, dy, itmax or tol");
+    cudaStream_t stream = static_cast<cudaStream_t>(stream_handle);
+
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        return error(CNV_NO_DEVICE, "no current CUDA device");
+    unsigned char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_mutex);
+        if (!g_scratch_addr[dev]) {
+            void* p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+            if (e != cudaSuccess || !p) return error(CNV_CUDA_ERROR, cudaGetErrorString(e));
+            g_scratch_addr[dev] = static_cast<unsigned char*>(p);
+        }
+        base = g_scratch_addr[dev];
+    }
+    Ctrl* ctrl = reinterpret_cast<Ctrl*>(base);
+    double* partials = reinterpret_cast<double*>(base + kCtrlBytes);
+    double* split = reinterpret_cast<double*>(base + kCtrlBytes + kPartialBytes);
+    const int pitch = ((n + 1) / 2 + 31) / 32 * 32;
+    const size_t split_elems = (size_t)n * pitch;  // <= kSplitBytes / 8
+    double* sor0 = split;
+    double* sor1 = split + kSplitBytes / sizeof(double);
+    double* rhs0 = split + 2 * (kSplitBytes / sizeof(double));
+    double* rhs1 = split + 3 * (kSplitBytes / sizeof(double));
+
+    // Same constants, evaluated the same way, as a cnv_state built for this grid.
+    PoissonParams p{};
+    p.n = n;
+    p.pitch = pitch;
+    p.kind = poisson_type;
+    p.arith = precision == CNV_PREC_FP64_FMA ? Arith::kFma : Arith::kExact;
+    p.itmax = itmax;
+    p.tol = tol;
+    const double pi = 3.14159265359;  // include/poisson.h:8
+    const double beta_ref = 0.5 * (2 / (1 + sin(pi / (n + 1))) + 2 / (1 + sin(pi / (n + 1))));
+    p.beta = poisson_type == CNV_POISSON_SOR ? (beta > 0 ? beta : beta_ref) : 1.0;
+    p.omb = 1 - p.beta;
+    p.dx2 = dx * dx;
+    p.dy2 = dy * dy;
+    p.den = 2 * (dx * dx + dy * dy);
+    int e2 = 0;
+    p.den_pow2 = std::frexp(p.den, &e2) == 0.5 ? 1 : 0;
+    p.rden = 1.0 / p.den;
+    p.wx = p.dx2 / p.den;
+    p.wy = p.dy2 / p.den;
+    p.timeout_ns = 2000000000LL;
+
+    StepArgs a{};
+    a.n = n;
+    a.pitch = pitch;
+    a.c4 = dx * dx * dy * dy;
+    a.rhs_mode = p.arith == Arith::kFma ? 1 : 0;
+    a.rhs_den = p.den;
+    a.rhs_rden = p.rden;
+    a.rhs_den_pow2 = p.den_pow2;
+
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, poisson_kernel_ptr(p.arith, p.kind),
+                                                      poisson_threads(), 0) != cudaSuccess ||
+        per_sm < 1)
+        return error(CNV_CUDA_ERROR, "device query failed");
+    const long long work = (long long)(n - 2) * ((n + 1) / 2);
+    long long grid = (work + 4LL * poisson_threads() - 1) / (4LL * poisson_threads());
+    grid = std::max(1LL, std::min(grid, std::min<long long>((long long)std::min(per_sm, 2) * sms, kMaxGrid)));
+
+    // Clear what must start at zero: psi (zero start, zero Dirichlet edge) and the control
+    // block (status, abort flag, barrier counter; no step records in this mode).
+    if (cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), stream) != cudaSuccess ||
+        cudaMemsetAsync(sor0, 0, split_elems * sizeof(double), stream) != cudaSuccess ||
+        cudaMemsetAsync(sor1, 0, split_elems * sizeof(double), stream) != cudaSuccess)
+        return error(CNV_CUDA_ERROR, "cudaMemsetAsync failed");
+    if (launch_to_split(f, rhs0, rhs1, a, stream) != cudaSuccess)
+        return error(CNV_CUDA_ERROR, "right-hand-side pass failed to launch");
+    PoissonLaunch L{};
+    L.p = p;
+    L.sor[0] = sor0;
+    L.sor[1] = sor1;
+    L.alt[0] = sor0;  // unused for GS/SOR
+    L.alt[1] = sor1;
+    L.rhs[0] = rhs0;
+    L.rhs[1] = rhs1;
+    L.ctrl = ctrl;
+    L.partials = partials;
+    L.grid = (int)grid;
+    const cudaError_t le = launch_poisson(L, stream);
+    if (le != cudaSuccess) return error(CNV_CUDA_ERROR, cudaGetErrorString(le));
+    if (launch_from_split(sor0, sor1, psi, n, pitch, stream) != cudaSuccess)
+        return error(CNV_CUDA_ERROR, "output pass failed to launch");
+    Ctrl h;
+    std::memset(&h, 0, sizeof h);
+    if (cudaMemcpyAsync(&h, ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess)
+        return error(CNV_CUDA_ERROR, "status read-back failed");
+    if (iters) *iters = h.iters;
+    if (err) *err = h.err;
+    if (h.status != CNV_OK) {
+        return error(h.status, h.status == CNV_NOT_CONVERGED ? "maximum number of iterations reached"
+                               : h.status == CNV_NONFINITE   ? "non-finite stop norm"
+                                                             : "solver status not OK");
+    }
+    return CNV_OK;
+}

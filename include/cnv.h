@@ -14,9 +14,6 @@
  * index (the lid is row i = n-1), exactly the flattening of src/linearalg.c:373-408. Host
  * pointers are plain host memory; *_device entry points take device pointers. One state is
  * used by one host thread at a time; each state owns one CUDA stream.
- *
- * The reference-shaped entry points (euler, poisson_SOR, ... with mtrx arguments) live in
- * cnv_compat.h.
  */
 #ifndef CNV_H
 #define CNV_H
@@ -156,6 +153,26 @@ int cnv_step_rows(cnv_state *s, double **w, double **u, double **v, double **psi
  * settings. iters/err may be NULL. */
 int cnv_poisson(cnv_state *s, const double *f, double *psi, int *iters, double *err);
 int cnv_poisson_device(cnv_state *s, const double *f, double *psi, int *iters, double *err);
+
+/* Poisson solve that allocates no device memory. No counterpart in the reference: it exists
+ * for callers that may not allocate GPU memory while they run, such as an application whose
+ * memory pool owns the whole device, or a real-time loop that forbids cudaMalloc/cudaFree
+ * (cudaFree synchronises the device and both calls take unbounded time).
+ * Same solve as cnv_poisson_device (psi = 0 start, psi = 0 on the edge, stop at
+ * sum |psi_k+1 - psi_k| < tol) on the CURRENT device, on stream (a cudaStream_t, NULL for the
+ * default stream), which is synchronised before return. f and psi are device arrays of n*n
+ * doubles, row-major; f is the right-hand side as poisson_SOR() takes it. poisson_type is
+ * CNV_POISSON_GS or CNV_POISSON_SOR; precision CNV_PREC_FP64 or CNV_PREC_FP64_FMA; beta <= 0
+ * selects the reference SOR factor for n. iters/err may be NULL.
+ * Working arrays live in one fixed array in device memory (about 4.2 MB, held by every GPU
+ * that loads the library until the process exits), so n is limited to 512: larger n returns
+ * CNV_BAD_ARG with a message on stderr. All calls on a device share that array: calls whose
+ * GPU work overlaps (other streams or host threads at the same time) race and must be
+ * serialised by the caller. The first call on each device sets up the array's address; make
+ * it before any stream capture. */
+int cnv_poisson_noalloc(const double *f, double *psi, int n, double dx, double dy,
+                        int poisson_type, int precision, double beta, int itmax, double tol,
+                        int *iters, double *err, void *stream);
 
 /* Statistics of the last cnv_step/cnv_poisson call: total Poisson sweeps, device time of the
  * whole call (ms, CUDA events on the state's stream) and device time of the Poisson kernel of
