@@ -40,7 +40,7 @@ class Config(C.Structure):
         ("sor_omega", C.c_double), ("nsteps", C.c_int), ("precision", C.c_int),
         ("mixed_rtol", C.c_double), ("init_field", C.c_int), ("seed", C.c_ulonglong),
         ("init_sigma", C.c_double), ("init_smooth_passes", C.c_int), ("device", C.c_int),
-        ("reserved", C.c_int * 8),
+        ("solver_blocks", C.c_int), ("reserved", C.c_int * 7),
     ]
 
 

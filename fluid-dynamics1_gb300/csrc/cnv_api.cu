@@ -77,7 +77,7 @@ struct cnv_state {
     double* alt[2] = {nullptr, nullptr};
     double* rhs[2] = {nullptr, nullptr};
     double* scratch = nullptr;   // 2*n*n: right-hand side and result of standalone Poisson solves
-    double* partials = nullptr;  // Poisson block partials
+    void* sync = nullptr;        // Poisson solver synchronisation state
     double* cont_partials = nullptr;
     int* flag = nullptr;         // non-finite scan result
     FdBands* bands = nullptr;
@@ -86,7 +86,7 @@ struct cnv_state {
     int max_records = 0;
 
     int cur = 0;                 // index of the current vorticity buffer
-    int poisson_grid = 0;
+    int poisson_grid = 0, poisson_gx = 1, poisson_gy = 1;
     int cont_blocks = 0;
     PoissonParams pp{};
     StepArgs sa{};
@@ -109,10 +109,11 @@ void free_state(cnv_state* s) {
         for (auto& g : row)
             if (g) cudaGraphExecDestroy(g);
     double* bufs[] = {s->w[0], s->w[1], s->u, s->v, s->psi, s->sor[0], s->sor[1], s->alt[0],
-                      s->alt[1], s->rhs[0], s->rhs[1], s->scratch, s->partials, s->cont_partials};
+                      s->alt[1], s->rhs[0], s->rhs[1], s->scratch, s->cont_partials};
     for (double* b : bufs)
         if (b) cudaFree(b);
     if (s->flag) cudaFree(s->flag);
+    if (s->sync) cudaFree(s->sync);
     if (s->bands) cudaFree(s->bands);
     if (s->ctrl) cudaFree(s->ctrl);
     if (s->records) cudaFree(s->records);
@@ -223,20 +224,21 @@ PoissonLaunch poisson_launch(cnv_state* s) {
         L.rhs[c] = s->rhs[c];
     }
     L.ctrl = s->ctrl;
-    L.partials = s->partials;
+    L.sync = s->sync;
     L.grid = s->poisson_grid;
+    L.gx = s->poisson_gx;
+    L.gy = s->poisson_gy;
     return L;
 }
 
 // Enqueue the Poisson solve on the split-layout rhs (psi starts from zero).
 int enqueue_poisson(cnv_state* s) {
     const size_t split_bytes = (size_t)s->n * s->pitch * 8;
+    // both copies of psi start at zero (zero start, zero Dirichlet edge)
     CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
     CNV_CUDA(cudaMemsetAsync(s->sor[1], 0, split_bytes, s->stream));
-    if (s->pp.kind == CNV_POISSON_JACOBI) {
-        CNV_CUDA(cudaMemsetAsync(s->alt[0], 0, split_bytes, s->stream));
-        CNV_CUDA(cudaMemsetAsync(s->alt[1], 0, split_bytes, s->stream));
-    }
+    CNV_CUDA(cudaMemsetAsync(s->alt[0], 0, split_bytes, s->stream));
+    CNV_CUDA(cudaMemsetAsync(s->alt[1], 0, split_bytes, s->stream));
     CNV_CUDA(launch_poisson(poisson_launch(s), s->stream));
     return CNV_OK;
 }
@@ -360,21 +362,32 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     ALLOC(s->ctrl, 1);
     ALLOC(s->flag, 1);
 
-    // Poisson solver geometry: co-resident blocks, at most 2 per SM, no more than the work needs
-    const void* kern = poisson_kernel_ptr(cfg->precision == CNV_PREC_FP64_FMA ? Arith::kFma : Arith::kExact,
-                                          cfg->poisson_type);
+    // Poisson arithmetic: the folded exact form needs dx = dy with dx^2 and 2*(dx^2+dy^2)
+    // powers of two (every n = 2^k on a unit cavity)
+    const double dx2 = s->dx * s->dx, dy2 = s->dy * s->dy;
+    const Arith arith = cfg->precision == CNV_PREC_FP64_FMA ? Arith::kFma : Arith::kExact;
+    const bool fold = arith == Arith::kExact && s->dx == s->dy && is_pow2(dx2) && is_pow2(2 * (dx2 + dy2));
+    // Poisson solver geometry: co-resident blocks (one tile each), a multiple of the SM count
+    const void* kern = poisson_kernel_ptr(arith, cfg->poisson_type, fold);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, poisson_threads(), 0) != cudaSuccess ||
         per_sm < 1) {
         free_state(s);
         return fail(CNV_CUDA_ERROR, "occupancy query failed for the Poisson kernel");
     }
-    const long long work = (long long)(n - 2) * W;
-    long long want = (work + 4LL * poisson_threads() - 1) / (4LL * poisson_threads());
-    const long long cap = (long long)std::min(per_sm, 2) * s->sms;
-    s->poisson_grid = (int)std::max(1LL, std::min(want, cap));
+    s->poisson_grid = poisson_grid_for(n, s->sms, per_sm);
+    if (cfg->solver_blocks > 0)
+        s->poisson_grid = std::min(cfg->solver_blocks, std::min(std::min(per_sm, 2) * s->sms, kMaxSolverBlocks));
+    poisson_tiles(n, s->poisson_grid, &s->poisson_gx, &s->poisson_gy);
+    s->poisson_grid = s->poisson_gx * s->poisson_gy;
     s->cont_blocks = (int)std::max(1LL, std::min<long long>(2LL * s->sms, (long long)(nn + 255) / 256));
-    ALLOC(s->partials, 2 * (size_t)s->poisson_grid);
+    {
+        cudaError_t e_ = cudaMalloc(&s->sync, poisson_sync_bytes());
+        if (e_ != cudaSuccess) {
+            free_state(s);
+            return fail(CNV_CUDA_ERROR, "cudaMalloc: %s", cudaGetErrorString(e_));
+        }
+    }
     ALLOC(s->cont_partials, 2 * (size_t)s->cont_blocks);
 #undef ALLOC
     if (cudaMemsetAsync(s->ctrl, 0, sizeof(Ctrl), s->stream) != cudaSuccess ||
@@ -400,7 +413,8 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     p.n = n;
     p.pitch = s->pitch;
     p.kind = cfg->poisson_type;
-    p.arith = cfg->precision == CNV_PREC_FP64_FMA ? Arith::kFma : Arith::kExact;
+    p.arith = arith;
+    p.fold = fold ? 1 : 0;
     p.itmax = cfg->poisson_max_it;
     p.tol = cfg->poisson_tol;
     // src/main.c:134 (PI of include/poisson.h:8); sor_omega > 0 overrides it
@@ -415,7 +429,8 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     p.rden = 1.0 / p.den;
     p.wx = p.dx2 / p.den;
     p.wy = p.dy2 / p.den;
-    p.timeout_ns = 2000000000LL;  // 2 s per barrier wait
+    p.b4 = p.beta / 4;
+    p.timeout_ns = 2000000000LL;  // 2 s per wait for another block
 
     StepArgs& a = s->sa;
     a.n = n;
@@ -432,10 +447,11 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     a.inv_re = 1. / cfg->Re;
     a.dt = cfg->dt;
     a.c4 = s->dx * s->dx * s->dy * s->dy;
-    a.rhs_mode = p.arith == Arith::kFma ? 1 : 0;
+    a.rhs_mode = p.arith == Arith::kFma ? 1 : (p.fold ? 2 : 0);
     a.rhs_den = p.den;
     a.rhs_rden = p.rden;
     a.rhs_den_pow2 = p.den_pow2;
+    a.rhs_inv_h2 = 1.0 / p.dx2;
     a.ctrl = s->ctrl;
     a.cont_partials = s->cont_partials;
     a.cont_blocks = s->cont_blocks;

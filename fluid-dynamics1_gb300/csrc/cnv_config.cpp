@@ -113,6 +113,7 @@ extern "C" int cnv_config_set(cnv_config* c, const char* key, const char* v) {
     else if (!strcmp(key, "init_sigma")) c->init_sigma = atof(v);
     else if (!strcmp(key, "init_smooth_passes")) c->init_smooth_passes = atoi(v);
     else if (!strcmp(key, "device")) c->device = atoi(v);
+    else if (!strcmp(key, "solver_blocks")) c->solver_blocks = atoi(v);
     else return CNV_BAD_ARG;
     return CNV_OK;
 }

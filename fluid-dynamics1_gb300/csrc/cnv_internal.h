@@ -6,9 +6,10 @@
 //   u, v          velocities, row-major n*n, as src/main.c:381-383 leaves them (derivatives of
 //                 psi on every cell; the Dirichlet values are applied on read, never stored)
 //   psi           streamfunction, row-major n*n (written by the velocity pass, for output)
-//   sor[2]        psi in red/black split layout: colour c = (i + j) & 1 of cell (i, j) lives
-//                 at sor[c][i * pitch + (j >> 1)]; a red cell's four neighbours are black and
-//                 vice versa, so every sweep reads and writes unit-stride rows
+//   sor[2],alt[2] psi in red/black split layout, two copies (sweeps alternate between them):
+//                 colour c = (i + j) & 1 of cell (i, j) lives at sor[c][i * pitch + (j >> 1)];
+//                 a red cell's four neighbours are black and vice versa, so every sweep reads and
+//                 writes unit-stride rows
 //   rhs[2]        the Poisson right-hand side in the same split layout, precomputed once per
 //                 step by the transport pass (c4 * f with f = -w, or its FMA-form scaling)
 //   coef          finite-difference bands: 7 row classes x 7 taps per operator
@@ -85,7 +86,9 @@ struct PoissonParams {
     double rden;        // 1/den when den is a power of two (then x/den == x*rden exactly)
     int den_pow2;
     double wx, wy;      // FMA form: dx2/den, dy2/den
-    long long timeout_ns;  // bound on every grid-barrier wait
+    double b4;          // beta / 4 (exact), folded exact form
+    int fold;           // 1: exact form with power-of-two scalings folded (dx = dy, dx^2 and den powers of 2)
+    long long timeout_ns;  // bound on every wait for another block
 };
 
 }  // namespace cnv

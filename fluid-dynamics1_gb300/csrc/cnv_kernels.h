@@ -24,10 +24,12 @@ struct StepArgs {
     double inv_re;             // 1. / Re as src/fluiddyn.c:98 evaluates it
     double dt;
     double c4;                 // dx*dx*dy*dy (src/poisson.c:247 evaluates it left to right)
-    int rhs_mode;              // 0: rhs = c4 * f; 1: rhs = (c4 * f) / den (FMA form)
+    int rhs_mode;              // 0: rhs = c4*f; 1: rhs = (c4*f) / den (FMA form);
+                               // 2: rhs = (c4*f) * (1/dx^2), an exact power-of-two scaling (folded form)
     double rhs_den;
     double rhs_rden;
     int rhs_den_pow2;
+    double rhs_inv_h2;
     Ctrl* ctrl;
     double* cont_partials;     // 2 * cont_blocks doubles
     int cont_blocks;
@@ -45,19 +47,29 @@ cudaError_t launch_from_split(const double* r, const double* b, double* f, int n
 // Scan n*n doubles for NaN/Inf; *flag (device int) is set to 1 when one is found.
 cudaError_t launch_nonfinite_scan(const double* x, long long count, int* flag, cudaStream_t s);
 
-// Persistent red-black Poisson solver (cooperative launch). sor/rhs are split-layout arrays;
-// alt is a second split pair used by Jacobi. grid = number of co-resident blocks.
+// Persistent Poisson solver (cooperative launch, one block per tile). sor/alt are the two
+// split-layout copies of psi (the answer ends in sor), rhs the split-layout right-hand side,
+// sync a buffer of poisson_sync_bytes() (zeroed by launch_poisson). grid = gx * gy blocks,
+// all co-resident.
+constexpr int kMaxSolverBlocks = 1024;
 struct PoissonLaunch {
     PoissonParams p;
     double* sor[2];
     double* alt[2];
     const double* rhs[2];
     Ctrl* ctrl;
-    double* partials;          // 2 * grid doubles
-    int grid;
+    void* sync;
+    int grid, gx, gy;
 };
 cudaError_t launch_poisson(const PoissonLaunch& L, cudaStream_t s);
 int poisson_threads();
-const void* poisson_kernel_ptr(Arith a, int kind);
+size_t poisson_sync_bytes();
+const void* poisson_kernel_ptr(Arith a, int kind, bool fold);
+// Tile factorisation grid = gx * gy for an n x n grid (tiles near-square, at least 64 wide when
+// possible).
+void poisson_tiles(int n, int grid, int* gx, int* gy);
+// Number of solver blocks for an n x n grid on a device with `sms` SMs that can hold `per_sm`
+// blocks per SM.
+int poisson_grid_for(int n, int sms, int per_sm);
 
 }  // namespace cnv

@@ -5,16 +5,16 @@
 // that forbids cudaMalloc/cudaFree after start-up. cudaFree synchronises the whole device and
 // both calls take unbounded time. Such a caller cannot create a cnv_state, because
 // cnv_create allocates the working buffers. cnv_poisson_noalloc takes only the caller's input
-// and output arrays and keeps every intermediate array (the red/black copies of psi and of the
-// right-hand side, the per-block partial sums, the control block) in the file-scope array
-// g_scratch below. The array is placed in device memory when the library's module is loaded,
+// and output arrays and keeps every intermediate array (the two red/black copies of psi, the
+// red/black right-hand side, the solver's synchronisation block, the control block) in the
+// file-scope array g_scratch below. The array is placed in device memory when the library's module is loaded,
 // and every GPU that loads the library keeps it until the process exits.
 //
 // Limits and sharing rules:
 //   - grids up to kMaxN x kMaxN (512 x 512); larger n is rejected with CNV_BAD_ARG;
-//   - Gauss-Seidel and SOR only (poisson_type 1 or 2); Jacobi would need a second psi copy;
 //   - all calls on a device share g_scratch, which keeps the previous call's contents. Each
-//     call clears what must start at zero (psi and the control block), so back-to-back calls
+//     call clears what must start at zero (psi, the control block and the solver's
+//     synchronisation block), so back-to-back calls
 //     are independent, but two calls whose GPU work overlaps (different streams or host
 //     threads at the same time) race on the same memory and give wrong results.
 //   - the first call on each device looks up the device address of g_scratch with
@@ -34,11 +34,10 @@ namespace {
 constexpr int kMaxN = 512;
 constexpr int kMaxPitch = ((kMaxN + 1) / 2 + 31) / 32 * 32;  // 256 doubles per split row
 constexpr size_t kSplitBytes = (size_t)kMaxN * kMaxPitch * sizeof(double);
-constexpr int kMaxGrid = 1024;                               // Poisson blocks
 constexpr size_t kCtrlBytes = 256;
-constexpr size_t kPartialBytes = 2 * kMaxGrid * sizeof(double);
-// control block | partials | psi red | psi black | rhs red | rhs black
-constexpr size_t kScratchBytes = kCtrlBytes + kPartialBytes + 4 * kSplitBytes;
+constexpr size_t kSyncBytes = 16384;                         // >= poisson_sync_bytes()
+// control block | solver sync | psi set 0 (red, black) | psi set 1 (red, black) | rhs (red, black)
+constexpr size_t kScratchBytes = kCtrlBytes + kSyncBytes + 6 * kSplitBytes;
 static_assert(sizeof(Ctrl) <= kCtrlBytes, "control block does not fit its slot");
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
@@ -65,8 +64,9 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
     if (!f || !psi) return error(CNV_BAD_ARG, "null input or output pointer");
     if (n < 3 || n > kMaxN)
         return error(CNV_BAD_ARG, "grid size n must be between 3 and 512 (the size of the built-in scratch array)");
-    if (poisson_type != CNV_POISSON_GS && poisson_type != CNV_POISSON_SOR)
-        return error(CNV_BAD_ARG, "poisson_type must be 1 (Gauss-Seidel) or 2 (SOR)");
+    if (poisson_type < CNV_POISSON_GS || poisson_type > CNV_POISSON_JACOBI)
+        return error(CNV_BAD_ARG, "poisson_type must be 1 (Gauss-Seidel), 2 (SOR) or 3 (Jacobi)");
+    if (poisson_sync_bytes() > kSyncBytes) return error(CNV_CUDA_ERROR, "solver sync block too large");
     if (precision != CNV_PREC_FP64 && precision != CNV_PREC_FP64_FMA)
         return error(CNV_BAD_ARG, "precision must be fp64 (0) or fp64_fma (1)");
     if (!(dx > 0) || !(dy > 0) || itmax < 1 || !(tol >= 0))
@@ -88,14 +88,17 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
         base = g_scratch_addr[dev];
     }
     Ctrl* ctrl = reinterpret_cast<Ctrl*>(base);
-    double* partials = reinterpret_cast<double*>(base + kCtrlBytes);
-    double* split = reinterpret_cast<double*>(base + kCtrlBytes + kPartialBytes);
+    void* sync = base + kCtrlBytes;
+    double* split = reinterpret_cast<double*>(base + kCtrlBytes + kSyncBytes);
     const int pitch = ((n + 1) / 2 + 31) / 32 * 32;
     const size_t split_elems = (size_t)n * pitch;  // <= kSplitBytes / 8
+    const size_t slot = kSplitBytes / sizeof(double);
     double* sor0 = split;
-    double* sor1 = split + kSplitBytes / sizeof(double);
-    double* rhs0 = split + 2 * (kSplitBytes / sizeof(double));
-    double* rhs1 = split + 3 * (kSplitBytes / sizeof(double));
+    double* sor1 = split + slot;
+    double* alt0 = split + 2 * slot;
+    double* alt1 = split + 3 * slot;
+    double* rhs0 = split + 4 * slot;
+    double* rhs1 = split + 5 * slot;
 
     // Same constants, evaluated the same way, as a cnv_state built for this grid.
     PoissonParams p{};
@@ -103,6 +106,11 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
     p.pitch = pitch;
     p.kind = poisson_type;
     p.arith = precision == CNV_PREC_FP64_FMA ? Arith::kFma : Arith::kExact;
+    auto pow2 = [](double x) {
+        int e;
+        return x > 0 && std::frexp(x, &e) == 0.5;
+    };
+    p.fold = (p.arith == Arith::kExact && dx == dy && pow2(dx * dx) && pow2(2 * (dx * dx + dy * dy))) ? 1 : 0;
     p.itmax = itmax;
     p.tol = tol;
     const double pi = 3.14159265359;  // include/poisson.h:8
@@ -117,32 +125,36 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
     p.rden = 1.0 / p.den;
     p.wx = p.dx2 / p.den;
     p.wy = p.dy2 / p.den;
+    p.b4 = p.beta / 4;
     p.timeout_ns = 2000000000LL;
 
     StepArgs a{};
     a.n = n;
     a.pitch = pitch;
     a.c4 = dx * dx * dy * dy;
-    a.rhs_mode = p.arith == Arith::kFma ? 1 : 0;
+    a.rhs_mode = p.arith == Arith::kFma ? 1 : (p.fold ? 2 : 0);
     a.rhs_den = p.den;
     a.rhs_rden = p.rden;
     a.rhs_den_pow2 = p.den_pow2;
+    a.rhs_inv_h2 = 1.0 / p.dx2;
 
     int sms = 0, per_sm = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, poisson_kernel_ptr(p.arith, p.kind),
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, poisson_kernel_ptr(p.arith, p.kind, p.fold != 0),
                                                       poisson_threads(), 0) != cudaSuccess ||
         per_sm < 1)
         return error(CNV_CUDA_ERROR, "device query failed");
-    const long long work = (long long)(n - 2) * ((n + 1) / 2);
-    long long grid = (work + 4LL * poisson_threads() - 1) / (4LL * poisson_threads());
-    grid = std::max(1LL, std::min(grid, std::min<long long>((long long)std::min(per_sm, 2) * sms, kMaxGrid)));
+    int gx = 1, gy = 1;
+    poisson_tiles(n, poisson_grid_for(n, sms, per_sm), &gx, &gy);
 
-    // Clear what must start at zero: psi (zero start, zero Dirichlet edge) and the control
-    // block (status, abort flag, barrier counter; no step records in this mode).
+    // Clear what must start at zero: both copies of psi (zero start, zero Dirichlet edge) and
+    // the control block (status, abort flag; no step records in this mode). launch_poisson
+    // clears the solver's sync block itself.
     if (cudaMemsetAsync(ctrl, 0, sizeof(Ctrl), stream) != cudaSuccess ||
         cudaMemsetAsync(sor0, 0, split_elems * sizeof(double), stream) != cudaSuccess ||
-        cudaMemsetAsync(sor1, 0, split_elems * sizeof(double), stream) != cudaSuccess)
+        cudaMemsetAsync(sor1, 0, split_elems * sizeof(double), stream) != cudaSuccess ||
+        cudaMemsetAsync(alt0, 0, split_elems * sizeof(double), stream) != cudaSuccess ||
+        cudaMemsetAsync(alt1, 0, split_elems * sizeof(double), stream) != cudaSuccess)
         return error(CNV_CUDA_ERROR, "cudaMemsetAsync failed");
     if (launch_to_split(f, rhs0, rhs1, a, stream) != cudaSuccess)
         return error(CNV_CUDA_ERROR, "right-hand-side pass failed to launch");
@@ -150,13 +162,15 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
     L.p = p;
     L.sor[0] = sor0;
     L.sor[1] = sor1;
-    L.alt[0] = sor0;  // unused for GS/SOR
-    L.alt[1] = sor1;
+    L.alt[0] = alt0;
+    L.alt[1] = alt1;
     L.rhs[0] = rhs0;
     L.rhs[1] = rhs1;
     L.ctrl = ctrl;
-    L.partials = partials;
-    L.grid = (int)grid;
+    L.sync = sync;
+    L.grid = gx * gy;
+    L.gx = gx;
+    L.gy = gy;
     const cudaError_t le = launch_poisson(L, stream);
     if (le != cudaSuccess) return error(CNV_CUDA_ERROR, cudaGetErrorString(le));
     if (launch_from_split(sor0, sor1, psi, n, pitch, stream) != cudaSuccess)

@@ -91,7 +91,8 @@ typedef struct cnv_config {
     double init_sigma;       /* CNV_INIT_NOISE standard deviation */
     int init_smooth_passes;  /* CNV_INIT_NOISE Jacobi averaging passes */
     int device;              /* CUDA device ordinal */
-    int reserved[8];
+    int solver_blocks;       /* Poisson solver blocks (tiles); <= 0 picks them from the grid size */
+    int reserved[7];
 } cnv_config;
 
 /* Per-step record: the values the reference logs (src/poisson.c:275, src/main.c:407-408). */
@@ -162,9 +163,9 @@ int cnv_poisson_device(cnv_state *s, const double *f, double *psi, int *iters, d
  * sum |psi_k+1 - psi_k| < tol) on the CURRENT device, on stream (a cudaStream_t, NULL for the
  * default stream), which is synchronised before return. f and psi are device arrays of n*n
  * doubles, row-major; f is the right-hand side as poisson_SOR() takes it. poisson_type is
- * CNV_POISSON_GS or CNV_POISSON_SOR; precision CNV_PREC_FP64 or CNV_PREC_FP64_FMA; beta <= 0
- * selects the reference SOR factor for n. iters/err may be NULL.
- * Working arrays live in one fixed array in device memory (about 4.2 MB, held by every GPU
+ * CNV_POISSON_GS, CNV_POISSON_SOR or CNV_POISSON_JACOBI; precision CNV_PREC_FP64 or
+ * CNV_PREC_FP64_FMA; beta <= 0 selects the reference SOR factor for n. iters/err may be NULL.
+ * Working arrays live in one fixed array in device memory (about 6.3 MB, held by every GPU
  * that loads the library until the process exits), so n is limited to 512: larger n returns
  * CNV_BAD_ARG with a message on stderr. All calls on a device share that array: calls whose
  * GPU work overlaps (other streams or host threads at the same time) race and must be

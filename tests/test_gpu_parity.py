@@ -62,6 +62,24 @@ def test_step_bitwise_equals_oracle(cnv, orc, n, order):
         assert bitwise(a["cont_max"], b["cont_max"]) and bitwise(a["cont_min"], b["cont_min"])
 
 
+@pytest.mark.parametrize("n,blocks", [(64, 4), (64, 16), (64, 37), (64, 152), (50, 9), (130, 304), (31, 6)])
+def test_step_bitwise_with_forced_tilings(cnv, orc, n, blocks):
+    """Many solver tiles on small grids: every tile frame and neighbour wait is exercised."""
+    cfg = make_cfg(cnv, n, solver_blocks=blocks, poisson_tol=1e-6)
+    g, gs, o, os_ = run_both(cnv, orc, cfg, 4)
+    for name, a, b in zip("w u v psi".split(), g, o):
+        assert bitwise(a, b), f"{name} differs: max abs {np.max(np.abs(a - b))}"
+    assert [s["iters"] for s in gs] == [s["iters"] for s in os_]
+
+
+@pytest.mark.parametrize("ptype", [1, 3])
+def test_gs_and_jacobi_steps_with_tiles(cnv, orc, ptype):
+    cfg = make_cfg(cnv, 48, poisson_type=ptype, solver_blocks=12, poisson_tol=1e-5, poisson_max_it=100000)
+    g, gs, o, os_ = run_both(cnv, orc, cfg, 3)
+    for name, a, b in zip("w u v psi".split(), g, o):
+        assert bitwise(a, b), name
+
+
 def test_step_all_boundary_values_and_rectangular_spacing(cnv, orc):
     cfg = make_cfg(cnv, 24, Lx=2, Ly=1, Re=400.0, dt=0.001, poisson_tol=1e-6, u1=0.1, u2=-0.2, u3=0.3,
                    u4=1.0, v1=0.05, v2=-0.05, v3=0.02, v4=-0.03, ui=0.01, vi=-0.02)

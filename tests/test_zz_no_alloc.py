@@ -30,7 +30,7 @@ def _solve_noalloc(cnv, torch, f_dev, psi_dev, n, h, ptype, precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("n,ptype,precision", [(200, 2, 0), (256, 2, 1), (97, 1, 0)])
+@pytest.mark.parametrize("n,ptype,precision", [(200, 2, 0), (256, 2, 1), (97, 1, 0), (128, 3, 0), (512, 2, 0)])
 def test_noalloc_matches_state_entry_point_on_two_calls(cnv, n, ptype, precision):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
@@ -65,6 +65,6 @@ def test_noalloc_rejects_grids_beyond_its_scratch_size(cnv):
     rc = cnv.load().cnv_poisson_noalloc(C.c_void_p(8), C.c_void_p(8), 513, 1 / 513, 1 / 513, 2, 0, 0.0,
                                         100, 1e-6, C.byref(it), C.byref(err), None)
     assert rc == cnv.CNV_BAD_ARG
-    rc = cnv.load().cnv_poisson_noalloc(C.c_void_p(8), C.c_void_p(8), 64, 1 / 64, 1 / 64, 3, 0, 0.0,
+    rc = cnv.load().cnv_poisson_noalloc(C.c_void_p(8), C.c_void_p(8), 64, 1 / 64, 1 / 64, 4, 0, 0.0,
                                         100, 1e-6, C.byref(it), C.byref(err), None)
     assert rc == cnv.CNV_BAD_ARG
