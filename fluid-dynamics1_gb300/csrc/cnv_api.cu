@@ -78,6 +78,15 @@ struct cnv_state {
     double* rhs[2] = {nullptr, nullptr};
     double* scratch = nullptr;   // 2*n*n: right-hand side and result of standalone Poisson solves
     void* sync = nullptr;        // Poisson solver synchronisation state
+    // mixed-precision form (CNV_PREC_MIXED)
+    bool mixed = false;
+    double* g = nullptr;         // c4*f, row-major
+    double* psi_w = nullptr;     // FP64 iterate, row-major
+    float* rq = nullptr;         // FP32 correction right-hand side, row-major
+    float* eg[2] = {nullptr, nullptr};  // FP32 correction border exchange, row-major
+    void* msync = nullptr;
+    int mixed_gx = 1, mixed_gy = 1, mixed_epochs = 1, mixed_max_outer = 100;
+    double mixed_rtol = 1e-10;
     double* cont_partials = nullptr;
     int* flag = nullptr;         // non-finite scan result
     FdBands* bands = nullptr;
@@ -109,9 +118,12 @@ void free_state(cnv_state* s) {
         for (auto& g : row)
             if (g) cudaGraphExecDestroy(g);
     double* bufs[] = {s->w[0], s->w[1], s->u, s->v, s->psi, s->sor[0], s->sor[1], s->alt[0],
-                      s->alt[1], s->rhs[0], s->rhs[1], s->scratch, s->cont_partials};
+                      s->alt[1], s->rhs[0], s->rhs[1], s->scratch, s->cont_partials, s->g, s->psi_w};
     for (double* b : bufs)
         if (b) cudaFree(b);
+    for (float* b : {s->rq, s->eg[0], s->eg[1]})
+        if (b) cudaFree(b);
+    if (s->msync) cudaFree(s->msync);
     if (s->flag) cudaFree(s->flag);
     if (s->sync) cudaFree(s->sync);
     if (s->bands) cudaFree(s->bands);
@@ -231,9 +243,44 @@ PoissonLaunch poisson_launch(cnv_state* s) {
     return L;
 }
 
-// Enqueue the Poisson solve on the split-layout rhs (psi starts from zero).
+MixedLaunch mixed_launch(cnv_state* s) {
+    MixedLaunch L{};
+    L.n = s->n;
+    L.pitch = s->pitch;
+    L.gx = s->mixed_gx;
+    L.gy = s->mixed_gy;
+    L.dx2 = s->pp.dx2;
+    L.dy2 = s->pp.dy2;
+    L.den = s->pp.den;
+    L.rden = 1.0 / s->pp.den;
+    L.beta = s->pp.beta;
+    L.rtol = s->mixed_rtol;
+    L.max_outer = s->mixed_max_outer;
+    L.epochs = s->mixed_epochs;
+    L.timeout_ns = s->pp.timeout_ns;
+    L.g = s->g;
+    L.psi = s->psi_w;
+    L.rq = s->rq;
+    L.eg[0] = s->eg[0];
+    L.eg[1] = s->eg[1];
+    L.sor[0] = s->sor[0];
+    L.sor[1] = s->sor[1];
+    L.ctrl = s->ctrl;
+    L.sync = s->msync;
+    return L;
+}
+
+// Enqueue the Poisson solve on the split-layout rhs, or on g for the mixed form (psi starts
+// from zero).
 int enqueue_poisson(cnv_state* s) {
     const size_t split_bytes = (size_t)s->n * s->pitch * 8;
+    if (s->mixed) {
+        CNV_CUDA(cudaMemsetAsync(s->psi_w, 0, (size_t)s->n * s->n * 8, s->stream));
+        CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
+        CNV_CUDA(cudaMemsetAsync(s->sor[1], 0, split_bytes, s->stream));
+        CNV_CUDA(launch_mixed(mixed_launch(s), s->stream));
+        return CNV_OK;
+    }
     // both copies of psi start at zero (zero start, zero Dirichlet edge)
     CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
     CNV_CUDA(cudaMemsetAsync(s->sor[1], 0, split_bytes, s->stream));
@@ -389,6 +436,44 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
         }
     }
     ALLOC(s->cont_partials, 2 * (size_t)s->cont_blocks);
+    if (cfg->precision == CNV_PREC_MIXED) {
+        // one block per SM; the tile plus its halo must fit in shared memory
+        s->mixed = true;
+        // every tile at least as wide and tall as the halo, so a halo comes from the eight
+        // adjacent tiles only
+        const int halo = 2 * mixed_sweeps_per_exchange();
+        for (int g = std::min(s->sms, kMaxSolverBlocks); g >= 1; --g) {
+            poisson_tiles(n, g, &s->mixed_gx, &s->mixed_gy);
+            if ((n - 2) / s->mixed_gx >= halo && (n - 2) / s->mixed_gy >= halo) break;
+            s->mixed_gx = s->mixed_gy = 1;
+        }
+        const size_t smem = mixed_smem_bytes(n, s->mixed_gx, s->mixed_gy);
+        if (smem + 2048 > prop.sharedMemPerBlockOptin) {
+            free_state(s);
+            return fail(CNV_BAD_ARG, "grid %d too large for the mixed form (tile needs %zu B of shared memory)", n,
+                        smem);
+        }
+        const int inner = cfg->mixed_inner_sweeps > 0 ? cfg->mixed_inner_sweeps : 2 * n;
+        s->mixed_epochs = std::max(1, (inner + mixed_sweeps_per_exchange() - 1) / mixed_sweeps_per_exchange());
+        s->mixed_max_outer = cfg->mixed_max_outer > 0 ? cfg->mixed_max_outer : 100;
+        s->mixed_rtol = cfg->mixed_rtol > 0 ? cfg->mixed_rtol : 1e-10;
+        ALLOC(s->g, nn);
+        ALLOC(s->psi_w, nn);
+        ALLOC(s->rq, nn);
+        ALLOC(s->eg[0], nn);
+        ALLOC(s->eg[1], nn);
+        cudaError_t e_ = cudaMalloc(&s->msync, mixed_sync_bytes());
+        if (e_ != cudaSuccess) {
+            free_state(s);
+            return fail(CNV_CUDA_ERROR, "cudaMalloc: %s", cudaGetErrorString(e_));
+        }
+        if (cudaMemsetAsync(s->g, 0, nn * 8, s->stream) != cudaSuccess ||
+            cudaMemsetAsync(s->eg[0], 0, nn * 4, s->stream) != cudaSuccess ||
+            cudaMemsetAsync(s->eg[1], 0, nn * 4, s->stream) != cudaSuccess) {
+            free_state(s);
+            return fail(CNV_CUDA_ERROR, "initial memset failed");
+        }
+    }
 #undef ALLOC
     if (cudaMemsetAsync(s->ctrl, 0, sizeof(Ctrl), s->stream) != cudaSuccess ||
         cudaMemsetAsync(s->rhs[0], 0, split * 8, s->stream) != cudaSuccess ||
@@ -455,6 +540,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     a.ctrl = s->ctrl;
     a.cont_partials = s->cont_partials;
     a.cont_blocks = s->cont_blocks;
+    a.g_rowmajor = s->mixed ? s->g : nullptr;
 
     if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess ||
         cudaEventCreate(&s->evp0) != cudaSuccess || cudaEventCreate(&s->evp1) != cudaSuccess) {
@@ -634,7 +720,10 @@ int cnv_poisson_device(cnv_state* s, const double* f, double* psi_out, int* iter
     int rc = ensure_records(s, 1);
     if (rc == CNV_OK) rc = reset_ctrl(s);
     if (rc != CNV_OK) return rc;
-    CNV_CUDA(launch_to_split(f, s->rhs[0], s->rhs[1], s->sa, s->stream));
+    if (s->mixed)
+        CNV_CUDA(launch_scale_rhs(f, s->g, s->n, s->sa.c4, s->stream));
+    else
+        CNV_CUDA(launch_to_split(f, s->rhs[0], s->rhs[1], s->sa, s->stream));
     CNV_CUDA(cudaEventRecord(s->ev0, s->stream));
     rc = enqueue_poisson(s);
     if (rc != CNV_OK) return rc;

@@ -114,6 +114,8 @@ extern "C" int cnv_config_set(cnv_config* c, const char* key, const char* v) {
     else if (!strcmp(key, "init_smooth_passes")) c->init_smooth_passes = atoi(v);
     else if (!strcmp(key, "device")) c->device = atoi(v);
     else if (!strcmp(key, "solver_blocks")) c->solver_blocks = atoi(v);
+    else if (!strcmp(key, "mixed_inner_sweeps")) c->mixed_inner_sweeps = atoi(v);
+    else if (!strcmp(key, "mixed_max_outer")) c->mixed_max_outer = atoi(v);
     else return CNV_BAD_ARG;
     return CNV_OK;
 }

@@ -84,15 +84,17 @@ typedef struct cnv_config {
     double sor_omega;        /* SOR factor; <= 0 selects the reference formula, src/main.c:134 */
     int nsteps;              /* steps to run; <= 0 selects (int)(tf/dt - 1) + 1, src/main.c:162 */
     int precision;           /* CNV_PREC_* */
-    double mixed_rtol;       /* CNV_PREC_MIXED: stop when ||f - A psi||_2 / ||f||_2 <= mixed_rtol;
-                                <= 0 keeps the reference stop rule (sum |d psi| < poisson_tol) */
+    double mixed_rtol;       /* CNV_PREC_MIXED: stop when ||f - A psi||_2 / ||f||_2 <= mixed_rtol
+                                (relative residual of the FP64 iterate); <= 0 selects 1e-10 */
     int init_field;          /* CNV_INIT_* */
     unsigned long long seed; /* CNV_INIT_NOISE generator seed (splitmix64) */
     double init_sigma;       /* CNV_INIT_NOISE standard deviation */
     int init_smooth_passes;  /* CNV_INIT_NOISE Jacobi averaging passes */
     int device;              /* CUDA device ordinal */
     int solver_blocks;       /* Poisson solver blocks (tiles); <= 0 picks them from the grid size */
-    int reserved[7];
+    int mixed_inner_sweeps;  /* CNV_PREC_MIXED: FP32 sweeps per correction; <= 0 picks 2*n */
+    int mixed_max_outer;     /* CNV_PREC_MIXED: correction limit (CNV_NOT_CONVERGED past it); <= 0: 100 */
+    int reserved[5];
 } cnv_config;
 
 /* Per-step record: the values the reference logs (src/poisson.c:275, src/main.c:407-408). */

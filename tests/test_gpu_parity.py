@@ -199,3 +199,57 @@ def test_reset_and_repeat_is_deterministic(cnv):
     assert s1 == s2
     for a, b in zip(f1, f2):
         assert bitwise(a, b)
+
+
+# ----------------------------------------------------------------------- mixed precision
+def fp64_residual(psi, f, Lx=1, Ly=1):
+    """||g - A psi||_2 / ||g||_2 over the interior, g = dx^2 dy^2 f (the reference's scaling)."""
+    n = psi.shape[0]
+    dx, dy = Lx / n, Ly / n
+    c4 = dx * dx * dy * dy
+    den = 2 * (dx * dx + dy * dy)
+    P = psi
+    ap = (dy * dy * (P[2:, 1:-1] + P[:-2, 1:-1]) + dx * dx * (P[1:-1, 2:] + P[1:-1, :-2])
+          - den * P[1:-1, 1:-1])
+    g = c4 * f[1:-1, 1:-1]
+    return np.linalg.norm(g - ap) / np.linalg.norm(g)
+
+
+MIXED_RTOL = 1e-10        # the mixed form's stop rule (relative FP64 residual)
+MIXED_FIELD_TOL = 1e-7    # mixed vs tightly converged FP64, normwise relative per field
+
+
+@pytest.mark.parametrize("n", [24, 64, 96, 256, 1024])
+def test_mixed_poisson_reaches_fp64_residual(cnv, orc, n):
+    rng = np.random.default_rng(n)
+    f = rng.standard_normal((n, n))
+    cfg = make_cfg(cnv, n, precision=cnv.PREC_MIXED, mixed_rtol=MIXED_RTOL)
+    with cnv.Cavity(cfg) as cav:
+        rc, psi, outer, rel = cav.poisson(f)
+    assert rc == 0, rel
+    assert rel <= MIXED_RTOL
+    assert fp64_residual(psi, f) <= 1.05 * MIXED_RTOL  # independent FP64 check of the iterate
+    assert np.all(psi[0, :] == 0) and np.all(psi[-1, :] == 0) and np.all(psi[:, 0] == 0) and np.all(psi[:, -1] == 0)
+    if n <= 256:
+        p = oracle_params(orc, cfg)
+        p.poisson_type, p.tol, p.itmax = 2, 1e-13 * n * n, 10_000_000
+        opsi, _, _, orc_rc = orc.poisson(p, f)
+        assert orc_rc == 0
+        assert np.max(np.abs(psi - opsi)) <= MIXED_FIELD_TOL * np.max(np.abs(opsi))
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_mixed_steps_match_fp64_fields(cnv, orc, n):
+    """Time steps with the mixed solve against the FP64 oracle run to a tight tolerance."""
+    cfg = make_cfg(cnv, n, precision=cnv.PREC_MIXED, mixed_rtol=MIXED_RTOL, dt=0.001)
+    with cnv.Cavity(cfg) as cav:
+        rc, steps = cav.step(5)
+        g = cav.get_fields()
+    assert rc == 0 and all(s["err"] <= MIXED_RTOL for s in steps)
+    p = oracle_params(orc, cfg)
+    p.tol = 1e-13 * n * n
+    p.itmax = 10_000_000
+    w, u, v, psi = orc.initial_state(n)
+    orc.run(p, 5, w, u, v, psi)
+    for name, a, b in zip("w u v psi".split(), g, (w, u, v, psi)):
+        assert np.max(np.abs(a - b)) <= MIXED_FIELD_TOL * np.max(np.abs(b)), name
