@@ -195,10 +195,18 @@ def profiled_traffic_per_launch():
 
 
 # ------------------------------------------------------------------------------- our arm
+FORMS = {
+    # name: (precision, description)
+    "fp64": (0, "fp64 (reference rounding)"),
+    "fp64_fma": (1, "fp64 (FMA form of the SOR update)"),
+    "mixed": (2, "FP32 red-black SOR sweeps inside FP64 defect correction to relative residual 1e-10"),
+}
+
+
 def make_config(cnvpy, w, device, precision=0):
     return cnvpy.default_config(nx=w["n"], ny=w["n"], Re=w["re"], u4=w["lid"], dt=w["dt"],
                                 poisson_tol=w["tol"], poisson_max_it=w["itmax"], device=device,
-                                precision=precision)
+                                precision=precision, mixed_rtol=1e-10)
 
 
 def run_device(cnvpy, w, device, steps, warmup, flush, precision=0, clocks=None):
@@ -277,7 +285,8 @@ def ours(args):
     flush = L2Flusher(local)
     clocks = ClockSampler(local) if rank == 0 else None
     dist.barrier()
-    recs = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=0, clocks=clocks)
+    prec, prec_name = FORMS[args.form]
+    recs = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=prec, clocks=clocks)
     clk = clocks.stop() if clocks else None
     dist.barrier()
     total_ms = sum(r["ms"] for r in recs)
@@ -288,9 +297,18 @@ def ours(args):
     interior = (w["n"] - 2) ** 2
     sweeps = sum(r["sweeps"] for r in recs)
     pms = sum(r["poisson_ms"] for r in recs)
-    achieved = sweeps * interior * BYTES_PER_CELL_SWEEP / (pms * 1e-3) / 1e9
+    if args.form == "mixed":
+        # FP32 sweep: read e and R/den, write e (12 B); per correction: FP64 residual (read psi,
+        # g, write R/den: 20 B) and update (read + write psi: 16 B)
+        outer = sum(r["iters"] for r in recs)
+        alg_bytes = interior * (12 * sweeps + 36 * outer)
+        kernel = "k_mixed (persistent FP32 red-black SOR in FP64 defect correction, one launch per step)"
+    else:
+        alg_bytes = interior * BYTES_PER_CELL_SWEEP * sweeps
+        kernel = "k_poisson (persistent red-black SOR, one launch per step)"
+    achieved = alg_bytes / (pms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = profiled_traffic_per_launch()
+    traffic = profiled_traffic_per_launch() if args.form == "fp64" else None
 
     e2e_s, pinned = run_e2e(cnvpy, w, local, args.steps, args.warmup)
     e2e_s = dist.max(e2e_s)
@@ -300,10 +318,14 @@ def ours(args):
 
     forms = {}
     if not args.skip_forms:
-        fma = run_device(cnvpy, w, local, max(2, args.steps // 4), 1, flush, precision=1)
-        f_ms = sum(r["ms"] for r in fma)
-        forms["fp64_fma"] = {"value": cells * len(fma) / (f_ms * 1e-3) / 1e6, "unit": UNIT,
-                             "steps": len(fma), "sweeps_per_step": sum(r["sweeps"] for r in fma) / len(fma)}
+        for name, (fprec, fdesc) in FORMS.items():
+            if name == args.form:
+                continue
+            fr = run_device(cnvpy, w, local, max(2, args.steps // 4), 1, flush, precision=fprec)
+            f_ms = sum(r["ms"] for r in fr)
+            forms[name] = {"value": round(cells * len(fr) / (f_ms * 1e-3) / 1e6, 4), "unit": UNIT,
+                           "steps": len(fr), "sweeps_per_step": sum(r["sweeps"] for r in fr) / len(fr),
+                           "solver": fdesc}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:
@@ -313,14 +335,14 @@ def ours(args):
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms_max / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(w), "grid": w["n"], "precision": "fp64 (reference rounding)",
+        "config": {"workload": workload_name(w), "grid": w["n"], "precision": prec_name,
                    "l2": "flushed before every timed step (256 MB device write)" if flush.active else "not flushed",
                    "parallelism": f"replicas x{ws}", "sweeps_per_step": round(sweeps / len(recs), 1),
                    "first_step": args.warmup},
         "Mcell_sweeps_per_s": round(interior * sweeps / (pms * 1e-3) / 1e6, 2),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": "k_poisson (persistent red-black SOR, one launch per step)"},
+                     "kernel": kernel},
         "e2e": e2e,
         "gpu_launches": 5 * args.steps,
         "clocks": clk,
@@ -381,6 +403,7 @@ def main():
     ap.add_argument("--n", type=int, default=1024, help=argparse.SUPPRESS)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--skip-forms", action="store_true", help="omit the extra precision/batch forms")
+    ap.add_argument("--form", choices=sorted(FORMS), default="fp64", help="form measured for the headline value")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least 3 untimed warm-up steps
     if args.impl == "reference":

@@ -80,12 +80,11 @@ struct cnv_state {
     void* sync = nullptr;        // Poisson solver synchronisation state
     // mixed-precision form (CNV_PREC_MIXED)
     bool mixed = false;
-    double* g = nullptr;         // c4*f, row-major
-    double* psi_w = nullptr;     // FP64 iterate, row-major
-    float* rq = nullptr;         // FP32 correction right-hand side, row-major
-    float* eg[2] = {nullptr, nullptr};  // FP32 correction border exchange, row-major
+    float* rq = nullptr;         // FP32 correction right-hand side (split layout, both colours)
+    float* eg = nullptr;         // FP32 correction border exchange (split layout, 2 parities x 2 colours)
     void* msync = nullptr;
     int mixed_gx = 1, mixed_gy = 1, mixed_epochs = 1, mixed_max_outer = 100;
+    bool mixed_rq_smem = false;
     double mixed_rtol = 1e-10;
     double* cont_partials = nullptr;
     int* flag = nullptr;         // non-finite scan result
@@ -118,10 +117,10 @@ void free_state(cnv_state* s) {
         for (auto& g : row)
             if (g) cudaGraphExecDestroy(g);
     double* bufs[] = {s->w[0], s->w[1], s->u, s->v, s->psi, s->sor[0], s->sor[1], s->alt[0],
-                      s->alt[1], s->rhs[0], s->rhs[1], s->scratch, s->cont_partials, s->g, s->psi_w};
+                      s->alt[1], s->rhs[0], s->rhs[1], s->scratch, s->cont_partials};
     for (double* b : bufs)
         if (b) cudaFree(b);
-    for (float* b : {s->rq, s->eg[0], s->eg[1]})
+    for (float* b : {s->rq, s->eg})
         if (b) cudaFree(b);
     if (s->msync) cudaFree(s->msync);
     if (s->flag) cudaFree(s->flag);
@@ -257,14 +256,15 @@ MixedLaunch mixed_launch(cnv_state* s) {
     L.rtol = s->mixed_rtol;
     L.max_outer = s->mixed_max_outer;
     L.epochs = s->mixed_epochs;
+    L.rq_in_smem = s->mixed_rq_smem ? 1 : 0;
     L.timeout_ns = s->pp.timeout_ns;
-    L.g = s->g;
-    L.psi = s->psi_w;
-    L.rq = s->rq;
-    L.eg[0] = s->eg[0];
-    L.eg[1] = s->eg[1];
-    L.sor[0] = s->sor[0];
-    L.sor[1] = s->sor[1];
+    const size_t split = (size_t)s->n * s->pitch;
+    for (int c = 0; c < 2; ++c) {
+        L.g[c] = s->rhs[c];
+        L.psi[c] = s->sor[c];
+        L.rq[c] = s->rq + c * split;
+        for (int par = 0; par < 2; ++par) L.eg[par][c] = s->eg + (2 * par + c) * split;
+    }
     L.ctrl = s->ctrl;
     L.sync = s->msync;
     return L;
@@ -275,7 +275,6 @@ MixedLaunch mixed_launch(cnv_state* s) {
 int enqueue_poisson(cnv_state* s) {
     const size_t split_bytes = (size_t)s->n * s->pitch * 8;
     if (s->mixed) {
-        CNV_CUDA(cudaMemsetAsync(s->psi_w, 0, (size_t)s->n * s->n * 8, s->stream));
         CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
         CNV_CUDA(cudaMemsetAsync(s->sor[1], 0, split_bytes, s->stream));
         CNV_CUDA(launch_mixed(mixed_launch(s), s->stream));
@@ -447,29 +446,26 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
             if ((n - 2) / s->mixed_gx >= halo && (n - 2) / s->mixed_gy >= halo) break;
             s->mixed_gx = s->mixed_gy = 1;
         }
-        const size_t smem = mixed_smem_bytes(n, s->mixed_gx, s->mixed_gy);
+        s->mixed_rq_smem = mixed_smem_bytes(n, s->mixed_gx, s->mixed_gy, true) + 2048 <= prop.sharedMemPerBlockOptin;
+        const size_t smem = mixed_smem_bytes(n, s->mixed_gx, s->mixed_gy, s->mixed_rq_smem);
         if (smem + 2048 > prop.sharedMemPerBlockOptin) {
             free_state(s);
             return fail(CNV_BAD_ARG, "grid %d too large for the mixed form (tile needs %zu B of shared memory)", n,
                         smem);
         }
-        const int inner = cfg->mixed_inner_sweeps > 0 ? cfg->mixed_inner_sweeps : 2 * n;
+        const int inner = cfg->mixed_inner_sweeps > 0 ? cfg->mixed_inner_sweeps : n;
         s->mixed_epochs = std::max(1, (inner + mixed_sweeps_per_exchange() - 1) / mixed_sweeps_per_exchange());
         s->mixed_max_outer = cfg->mixed_max_outer > 0 ? cfg->mixed_max_outer : 100;
         s->mixed_rtol = cfg->mixed_rtol > 0 ? cfg->mixed_rtol : 1e-10;
-        ALLOC(s->g, nn);
-        ALLOC(s->psi_w, nn);
-        ALLOC(s->rq, nn);
-        ALLOC(s->eg[0], nn);
-        ALLOC(s->eg[1], nn);
+        ALLOC(s->rq, 2 * split);
+        ALLOC(s->eg, 4 * split);
         cudaError_t e_ = cudaMalloc(&s->msync, mixed_sync_bytes());
         if (e_ != cudaSuccess) {
             free_state(s);
             return fail(CNV_CUDA_ERROR, "cudaMalloc: %s", cudaGetErrorString(e_));
         }
-        if (cudaMemsetAsync(s->g, 0, nn * 8, s->stream) != cudaSuccess ||
-            cudaMemsetAsync(s->eg[0], 0, nn * 4, s->stream) != cudaSuccess ||
-            cudaMemsetAsync(s->eg[1], 0, nn * 4, s->stream) != cudaSuccess) {
+        if (cudaMemsetAsync(s->rq, 0, 2 * split * 4, s->stream) != cudaSuccess ||
+            cudaMemsetAsync(s->eg, 0, 4 * split * 4, s->stream) != cudaSuccess) {
             free_state(s);
             return fail(CNV_CUDA_ERROR, "initial memset failed");
         }
@@ -532,7 +528,8 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     a.inv_re = 1. / cfg->Re;
     a.dt = cfg->dt;
     a.c4 = s->dx * s->dx * s->dy * s->dy;
-    a.rhs_mode = p.arith == Arith::kFma ? 1 : (p.fold ? 2 : 0);
+    // the mixed form takes g = c4*f as it is; the FP64 forms take their scaled variants
+    a.rhs_mode = s->mixed ? 0 : (p.arith == Arith::kFma ? 1 : (p.fold ? 2 : 0));
     a.rhs_den = p.den;
     a.rhs_rden = p.rden;
     a.rhs_den_pow2 = p.den_pow2;
@@ -540,7 +537,6 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     a.ctrl = s->ctrl;
     a.cont_partials = s->cont_partials;
     a.cont_blocks = s->cont_blocks;
-    a.g_rowmajor = s->mixed ? s->g : nullptr;
 
     if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess ||
         cudaEventCreate(&s->evp0) != cudaSuccess || cudaEventCreate(&s->evp1) != cudaSuccess) {
@@ -720,10 +716,7 @@ int cnv_poisson_device(cnv_state* s, const double* f, double* psi_out, int* iter
     int rc = ensure_records(s, 1);
     if (rc == CNV_OK) rc = reset_ctrl(s);
     if (rc != CNV_OK) return rc;
-    if (s->mixed)
-        CNV_CUDA(launch_scale_rhs(f, s->g, s->n, s->sa.c4, s->stream));
-    else
-        CNV_CUDA(launch_to_split(f, s->rhs[0], s->rhs[1], s->sa, s->stream));
+    CNV_CUDA(launch_to_split(f, s->rhs[0], s->rhs[1], s->sa, s->stream));
     CNV_CUDA(cudaEventRecord(s->ev0, s->stream));
     rc = enqueue_poisson(s);
     if (rc != CNV_OK) return rc;

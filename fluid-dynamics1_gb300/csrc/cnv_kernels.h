@@ -33,7 +33,6 @@ struct StepArgs {
     Ctrl* ctrl;
     double* cont_partials;     // 2 * cont_blocks doubles
     int cont_blocks;
-    double* g_rowmajor;        // mixed form: rhs c4*f row-major (nullptr: split layout only)
 };
 
 cudaError_t launch_wall(const StepArgs& a, cudaStream_t s);
@@ -67,29 +66,28 @@ int poisson_threads();
 size_t poisson_sync_bytes();
 const void* poisson_kernel_ptr(Arith a, int kind, bool fold);
 // Mixed-precision solve (cnv_mixed.cu): FP32 red-black SOR sweeps inside FP64 defect
-// correction. g = c4*f row-major (input), psi row-major FP64 work copy (zeroed by the caller for
-// a zero start), rq/eg FP32 row-major work arrays, sor = split-layout output for the velocity
-// pass, sync = mixed_sync_bytes() (zeroed by launch_mixed). One block per tile, gx*gy blocks.
+// correction. Every array is in the red/black split layout (pitch doubles or floats per row):
+// g = c4*f (input), psi = the FP64 iterate and the answer (zeroed by the caller for a zero
+// start), rq / eg = FP32 work arrays (correction right-hand side; border-exchange copies by
+// epoch parity). sync = mixed_sync_bytes() (zeroed by launch_mixed). gx*gy blocks, one per tile.
 struct MixedLaunch {
     int n, pitch, gx, gy;
     double dx2, dy2, den, rden, beta, rtol;
     int max_outer, epochs;
+    int rq_in_smem;   // keep the correction right-hand side tile in shared memory
     long long timeout_ns;
-    const double* g;
-    double* psi;
-    float* rq;
-    float* eg[2];
-    double* sor[2];
+    const double* g[2];
+    double* psi[2];
+    float* rq[2];
+    float* eg[2][2];  // [parity][colour]
     Ctrl* ctrl;
     void* sync;
 };
 cudaError_t launch_mixed(const MixedLaunch& L, cudaStream_t s);
 size_t mixed_sync_bytes();
-size_t mixed_smem_bytes(int n, int gx, int gy);
+size_t mixed_smem_bytes(int n, int gx, int gy, bool rq_in_smem);
 int mixed_threads();
 int mixed_sweeps_per_exchange();
-// g = c4 * f (row-major, interior only; zero on the edge), for standalone mixed solves
-cudaError_t launch_scale_rhs(const double* f, double* g, int n, double c4, cudaStream_t s);
 
 // Tile factorisation grid = gx * gy for an n x n grid (tiles near-square, at least 64 wide when
 // possible).

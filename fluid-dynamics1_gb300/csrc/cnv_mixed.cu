@@ -8,20 +8,26 @@
 // on the interior, psi = 0 on the edge, den = 2 (dx^2 + dy^2). Defect correction:
 //     psi = 0 (FP64)
 //     loop: R = g - A psi (FP64); stop when ||R||_2 <= rtol ||g||_2
-//           solve A e = R approximately with `inner` FP32 red-black SOR sweeps from e = 0
+//           solve A e = R approximately with `epochs * kSweepsPerExchange` FP32 red-black SOR
+//           sweeps from e = 0
 //           psi += e (FP64)
 // Only the residual, the norm and the correction accumulation are FP64; every sweep is FP32.
 //
-// Inner sweeps. Each block owns one tile and keeps its correction e for the tile plus a halo of
-// width H = 2*kSweepsPerExchange in shared memory. An "epoch" is kSweepsPerExchange red-black
-// sweeps done entirely in shared memory: half-sweep s updates its colour on the tile grown by
-// H - s cells on every side (clipped to the interior), so after 2*kSweepsPerExchange half-sweeps
-// the tile itself holds exactly what global red-black SOR would hold. The redundant halo work is
-// the price of talking to neighbours once per epoch instead of once per half-sweep. At an epoch's
-// end every block writes its border strips (width H) into a global FP32 copy of e
-// (double-buffered by epoch parity) and raises its flag; the next epoch starts by waiting for the
-// eight neighbours' flags and loading their strips into the halo. The right-hand side of the
-// correction (R / den, FP32) is read from global memory (L2) on every update.
+// Layout. g, psi, the FP32 correction right-hand side R/den and the FP32 border-exchange copies
+// of e all use the red/black split layout of the rest of the library (colour c = (i+j)&1 of cell
+// (i, j) at A_c[i*pitch + (j>>1)]), and so does the shared-memory tile: every access in a sweep
+// is unit-stride, and warps walk whole rows, so no integer division is needed per cell.
+//
+// Inner sweeps. Each block owns one tile and keeps e on the tile plus a halo of width
+// H = 2*kSweepsPerExchange in shared memory. An "epoch" is kSweepsPerExchange red-black sweeps
+// done entirely in shared memory: half-sweep s updates its colour on the tile grown by H - s
+// cells on every side (clipped to the interior), so after 2*kSweepsPerExchange half-sweeps the
+// tile holds exactly what global red-black SOR would hold. The redundant halo work buys one
+// neighbour exchange per epoch instead of one per half-sweep. At an epoch's end every block
+// writes its border strips (width H) into a global FP32 copy of e (double-buffered by epoch
+// parity) and raises its flag; the next epoch waits for the eight neighbours' flags and loads
+// their strips into the halo. Tiles are at least H cells wide and tall, so a halo only ever
+// comes from the eight adjacent tiles.
 //
 // All waits are bounded (timeout + abort flag) and report CNV_TIMEOUT instead of hanging.
 #include <algorithm>
@@ -32,7 +38,8 @@
 namespace cnv {
 namespace {
 
-constexpr int kThreads = 512;
+constexpr int kThreads = 1024;
+constexpr int kWarps = kThreads / 32;
 constexpr int kSweepsPerExchange = 4;
 constexpr int kHalo = 2 * kSweepsPerExchange;
 
@@ -90,7 +97,7 @@ __device__ bool grid_sync(MixedSync* sy, unsigned& epoch, Ctrl* ctl, long long t
 
 struct MTile {
     int r0, r1, c0, c1;  // owned rows/cols (absolute)
-    int nb[8];           // neighbour blocks (ty-1..ty+1, tx-1..tx+1 without self), -1 if none
+    int nb[8];           // the eight adjacent tiles' blocks, -1 where there is none
 };
 
 __device__ __forceinline__ MTile make_mtile(int n, int gx, int gy, int b) {
@@ -111,36 +118,82 @@ __device__ __forceinline__ MTile make_mtile(int n, int gx, int gy, int b) {
     return t;
 }
 
+__host__ __device__ __forceinline__ int floor_half(int j) { return j >= 0 ? j / 2 : -((1 - j) / 2); }
+
+// Shared-memory tile in split layout: rows sr0 .. sr0+sh-1, global split columns m0 .. m0+swm-1.
+struct SmemTile {
+    int sr0, sh, m0, swm;
+    float* c[2];
+    __device__ __forceinline__ float& at(int col, int i, int m) const { return c[col][(i - sr0) * swm + (m - m0)]; }
+};
+
 }  // namespace
 
 size_t mixed_sync_bytes() { return sizeof(MixedSync); }
 
-// Shared-memory bytes the mixed kernel needs for the largest tile of a gx x gy tiling of n.
-size_t mixed_smem_bytes(int n, int gx, int gy) {
+// Shared-memory bytes the mixed kernel needs for the largest tile of a gx x gy tiling of n:
+// e (both colours) on the tile plus halo, and the same again when the correction right-hand side
+// is also kept there (rq_in_smem).
+size_t mixed_smem_bytes(int n, int gx, int gy, bool rq_in_smem) {
     const int ni = n - 2;
     const int tw = (ni + gx - 1) / gx + 2 * kHalo;
     const int th = (ni + gy - 1) / gy + 2 * kHalo;
-    return (size_t)tw * th * sizeof(float);
+    const int swm = tw / 2 + 2;
+    return (rq_in_smem ? 4 : 2) * (size_t)th * swm * sizeof(float);
 }
 
 namespace {
 
+// One colour c of an FP32 red-black SOR half-sweep on rows [lo_r, hi_r), columns [lo_c, hi_c) of
+// the shared-memory tile (split layout: row r of colour k at sc/so[(i - sr0) * swm + (m - m0)]).
+// The correction right-hand side comes from the shared-memory tile (RQ_SMEM) or from L2. Kept
+// out of line so that it gets its own register allocation: it is the hot loop of the solve.
+template <bool RQ_SMEM>
+__device__ __noinline__ void mixed_half_sweep(float* __restrict__ sc, const float* __restrict__ so,
+                                              const float* __restrict__ rq, int sr0, int swm, int m0,
+                                              int lo_r, int hi_r, int lo_c, int hi_c, int c, int P,
+                                              float wx, float wy, float beta) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = lo_r + warp; i < hi_r; i += kWarps) {
+        const int q = (i + c) & 1;
+        const int mlo = floor_half(lo_c - q + 1), mhi = floor_half(hi_c - 1 - q);
+        const int row = (i - sr0) * swm - m0;
+        const float* rqrow = RQ_SMEM ? rq + row : rq + (size_t)i * P;
+        for (int m = mlo + lane; m <= mhi; m += 32) {
+            const float up = so[row + swm + m], dn = so[row - swm + m];
+            const float lt = so[row + m - 1 + q], rt = so[row + m + q];
+            // R/den: shared-memory copy, or L2 (rewritten every outer iteration)
+            const float r = RQ_SMEM ? rqrow[m] : __ldcg(rqrow + m);
+            const float me = sc[row + m];
+            const float gs = fmaf(wy, up + dn, fmaf(wx, lt + rt, -r));
+            sc[row + m] = fmaf(beta, gs - me, me);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
     Ctrl* ctl = L.ctrl;
     if (ctl->abort) return;
-    extern __shared__ float s_e[];
+    extern __shared__ float s_mem[];
     __shared__ int s_ok;
     __shared__ int s_flag[8];
-    __shared__ double s_red[kThreads / 32][2];
+    __shared__ double s_red[kWarps][2];
     __shared__ double s_tot[2];
     MixedSync* sy = reinterpret_cast<MixedSync*>(L.sync);
-    const int n = L.n;
+    const int n = L.n, P = L.pitch;
     const MTile t = make_mtile(n, L.gx, L.gy, blockIdx.x);
-    // shared tile geometry: rows r0-H .. r1+H-1, cols c0-H .. c1+H-1
-    const int sr0 = t.r0 - kHalo, sc0 = t.c0 - kHalo;
-    const int sh = t.r1 - t.r0 + 2 * kHalo, sw = t.c1 - t.c0 + 2 * kHalo;
-    const int ssz = sh * sw;
-    auto S = [&](int i, int j) -> float& { return s_e[(i - sr0) * sw + (j - sc0)]; };
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    SmemTile S;
+    S.sr0 = t.r0 - kHalo;
+    S.sh = t.r1 - t.r0 + 2 * kHalo;
+    S.m0 = floor_half(t.c0 - kHalo);
+    S.swm = floor_half(t.c1 + kHalo - 1) - S.m0 + 1;
+    S.c[0] = s_mem;
+    S.c[1] = s_mem + S.sh * S.swm;
+    const int ssz = 2 * S.sh * S.swm;
+    // correction right-hand side tile (both colours) after e, when it fits in shared memory
+    float* const srq = L.rq_in_smem ? s_mem + ssz : nullptr;
 
     const double dx2 = L.dx2, dy2 = L.dy2, den = L.den;
     const float wx = (float)(dx2 / den), wy = (float)(dy2 / den), beta = (float)L.beta;
@@ -152,32 +205,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
     for (outer = 0;; ++outer) {
         // ---- FP64 residual R = g - A psi on own cells, its norm, and the FP32 rhs R/den
         double rr = 0.0, gg = 0.0;
-        const int ow = t.c1 - t.c0, oh = t.r1 - t.r0;
-        for (int x = threadIdx.x; x < ow * oh; x += kThreads) {
-            const int i = t.r0 + x / ow, j = t.c0 + x % ow;
-            const size_t k = (size_t)i * n + j;
-            const double* P = L.psi;
-            const double ap = dy2 * (__ldcg(P + k + n) + __ldcg(P + k - n)) +
-                              dx2 * (__ldcg(P + k + 1) + __ldcg(P + k - 1)) - den * __ldcg(P + k);
-            const double g = L.g[k];
-            const double R = g - ap;
-            rr = fma(R, R, rr);
-            if (outer == 0) gg = fma(g, g, gg);
-            L.rq[k] = (float)(R * L.rden);
+        for (int i = t.r0 + warp; i < t.r1; i += kWarps) {
+            for (int c = 0; c < 2; ++c) {
+                const int q = (i + c) & 1;  // cell (i, j) of colour c has j = 2m + q
+                const int mlo = floor_half(t.c0 - q + 1), mhi = floor_half(t.c1 - 1 - q);
+                const double* pc = L.psi[c];
+                const double* po = L.psi[c ^ 1];
+                for (int m = mlo + lane; m <= mhi; m += 32) {
+                    const size_t k = (size_t)i * P + m;
+                    const double ap = dy2 * (__ldcg(po + k + P) + __ldcg(po + k - P)) +
+                                      dx2 * (__ldcg(po + k - 1 + q) + __ldcg(po + k + q)) - den * __ldcg(pc + k);
+                    const double g = L.g[c][k];
+                    const double R = g - ap;
+                    rr = fma(R, R, rr);
+                    if (outer == 0) gg = fma(g, g, gg);
+                    L.rq[c][k] = (float)(R * L.rden);
+                }
+            }
         }
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
             rr += __shfl_xor_sync(0xffffffffu, rr, off);
             gg += __shfl_xor_sync(0xffffffffu, gg, off);
         }
-        if ((threadIdx.x & 31) == 0) {
-            s_red[threadIdx.x >> 5][0] = rr;
-            s_red[threadIdx.x >> 5][1] = gg;
+        if (lane == 0) {
+            s_red[warp][0] = rr;
+            s_red[warp][1] = gg;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             double a = 0.0, b = 0.0;
-            for (int w = 0; w < kThreads / 32; ++w) {
+            for (int w = 0; w < kWarps; ++w) {
                 a += s_red[w][0];
                 b += s_red[w][1];
             }
@@ -208,9 +266,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
         if (!isfinite(rel)) { status = CNV_NONFINITE; break; }
         if (rel <= L.rtol) { status = CNV_OK; break; }
         if (outer >= L.max_outer) break;
+        if (srq) {
+            // R/den on the tile plus halo (every block wrote its own cells before the barrier)
+            for (int r = warp; r < S.sh; r += kWarps) {
+                const int i = S.sr0 + r;
+                for (int c = 0; c < 2; ++c) {
+                    const int q = (i + c) & 1;
+                    float* dst = srq + c * (S.sh * S.swm) + r * S.swm;
+                    for (int mm = lane; mm < S.swm; mm += 32) {
+                        const int j = 2 * (S.m0 + mm) + q;
+                        dst[mm] = (i >= 1 && i <= n - 2 && j >= 1 && j <= n - 2)
+                                      ? __ldcg(L.rq[c] + (size_t)i * P + S.m0 + mm)
+                                      : 0.0f;
+                    }
+                }
+            }
+            __syncthreads();
+        }
 
         // ---- FP32 inner solve: e = 0, then `epochs` epochs of kSweepsPerExchange sweeps
-        for (int x = threadIdx.x; x < ssz; x += kThreads) s_e[x] = 0.0f;
+        for (int x = threadIdx.x; x < ssz; x += kThreads) s_mem[x] = 0.0f;
         __syncthreads();
         bool ok = true;
         for (int e = 0; e < L.epochs && ok; ++e) {
@@ -224,12 +299,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
                 __syncthreads();
                 for (int q = 0; q < 8; ++q) ok = ok && s_flag[q];
                 if (!ok) break;
-                const float* eg = L.eg[(ep - 1) & 1];
-                for (int x = threadIdx.x; x < ssz; x += kThreads) {
-                    const int i = sr0 + x / sw, j = sc0 + x % sw;
-                    const bool own = i >= t.r0 && i < t.r1 && j >= t.c0 && j < t.c1;
-                    if (own || i < 1 || i > n - 2 || j < 1 || j > n - 2) continue;
-                    s_e[x] = __ldcg(eg + (size_t)i * n + j);
+                const int par = (ep - 1) & 1;
+                for (int r = warp; r < S.sh; r += kWarps) {
+                    const int i = S.sr0 + r;
+                    if (i < 1 || i > n - 2) continue;
+                    const bool own_row = i >= t.r0 && i < t.r1;
+                    for (int c = 0; c < 2; ++c) {
+                        const int q = (i + c) & 1;
+                        const float* src = L.eg[par][c] + (size_t)i * P;
+                        // halo columns of this row: all of [c0-H, c1+H) for rows outside the
+                        // tile, else the two side strips; clipped to the interior
+                        for (int seg = 0; seg < (own_row ? 2 : 1); ++seg) {
+                            int jlo = own_row ? (seg ? t.c1 : t.c0 - kHalo) : t.c0 - kHalo;
+                            int jhi = own_row ? (seg ? t.c1 + kHalo : t.c0) : t.c1 + kHalo;
+                            jlo = max(jlo, 1);
+                            jhi = min(jhi, n - 1);
+                            const int mlo = floor_half(jlo - q + 1), mhi = floor_half(jhi - 1 - q);
+                            for (int m = mlo + lane; m <= mhi; m += 32) S.at(c, i, m) = __ldcg(src + m);
+                        }
+                    }
                 }
                 __syncthreads();
             }
@@ -237,29 +325,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
                 const int c = (s - 1) & 1;  // red first
                 const int lo_r = max(1, t.r0 - kHalo + s), hi_r = min(n - 1, t.r1 + kHalo - s);
                 const int lo_c = max(1, t.c0 - kHalo + s), hi_c = min(n - 1, t.c1 + kHalo - s);
-                const int rw = hi_c - lo_c, rh = hi_r - lo_r;
-                const int rq_w = (rw + 1) >> 1;
-                for (int x = threadIdx.x; x < rh * rq_w; x += kThreads) {
-                    const int r = x / rq_w;
-                    const int i = lo_r + r;
-                    const int j = lo_c + 2 * (x - r * rq_w) + ((i + lo_c + c) & 1);
-                    if (j >= hi_c) continue;
-                    float& me = S(i, j);
-                    const float up = S(i + 1, j), dn = S(i - 1, j), lt = S(i, j - 1), rt = S(i, j + 1);
-                    const float rq = __ldcg(L.rq + (size_t)i * n + j);  // rewritten every outer iteration
-                    const float gs = fmaf(wy, up + dn, fmaf(wx, lt + rt, -rq));
-                    me = fmaf(beta, gs - me, me);
-                }
+                if (srq)
+                    mixed_half_sweep<true>(S.c[c], S.c[c ^ 1], srq + c * (S.sh * S.swm), S.sr0, S.swm, S.m0,
+                                           lo_r, hi_r, lo_c, hi_c, c, P, wx, wy, beta);
+                else
+                    mixed_half_sweep<false>(S.c[c], S.c[c ^ 1], L.rq[c], S.sr0, S.swm, S.m0, lo_r, hi_r,
+                                            lo_c, hi_c, c, P, wx, wy, beta);
                 __syncthreads();
             }
             sweeps += kSweepsPerExchange;
             if (e + 1 < L.epochs) {
                 // own border strips (width H) -> global copy of this epoch; raise the flag
-                float* eg = L.eg[ep & 1];
-                for (int x = threadIdx.x; x < ow * oh; x += kThreads) {
-                    const int i = t.r0 + x / ow, j = t.c0 + x % ow;
-                    if (i >= t.r0 + kHalo && i < t.r1 - kHalo && j >= t.c0 + kHalo && j < t.c1 - kHalo) continue;
-                    eg[(size_t)i * n + j] = S(i, j);
+                const int par = ep & 1;
+                for (int i = t.r0 + warp; i < t.r1; i += kWarps) {
+                    const bool edge_row = i < t.r0 + kHalo || i >= t.r1 - kHalo;
+                    for (int c = 0; c < 2; ++c) {
+                        const int q = (i + c) & 1;
+                        float* dst = L.eg[par][c] + (size_t)i * P;
+                        // border columns: the whole row near the top/bottom edge, else the two
+                        // side strips of width H
+                        for (int seg = 0; seg < (edge_row ? 1 : 2); ++seg) {
+                            const int jlo = edge_row ? t.c0 : (seg ? max(t.c1 - kHalo, t.c0) : t.c0);
+                            const int jhi = edge_row ? t.c1 : (seg ? t.c1 : min(t.c0 + kHalo, t.c1));
+                            const int mlo = floor_half(jlo - q + 1), mhi = floor_half(jhi - 1 - q);
+                            for (int m = mlo + lane; m <= mhi; m += 32) dst[m] = S.at(c, i, m);
+                        }
+                    }
                 }
                 __syncthreads();
                 if (threadIdx.x == 0) st_release(&sy->flag[blockIdx.x], ep);
@@ -267,21 +358,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
         }
         if (!ok) { status = CNV_TIMEOUT; break; }
         // ---- FP64 correction psi += e on own cells
-        for (int x = threadIdx.x; x < ow * oh; x += kThreads) {
-            const int i = t.r0 + x / ow, j = t.c0 + x % ow;
-            L.psi[(size_t)i * n + j] += (double)S(i, j);
+        for (int i = t.r0 + warp; i < t.r1; i += kWarps) {
+            for (int c = 0; c < 2; ++c) {
+                const int q = (i + c) & 1;
+                const int mlo = floor_half(t.c0 - q + 1), mhi = floor_half(t.c1 - 1 - q);
+                double* pc = L.psi[c];
+                for (int m = mlo + lane; m <= mhi; m += 32) pc[(size_t)i * P + m] += (double)S.at(c, i, m);
+            }
         }
         if (!grid_sync(sy, bar, ctl, L.timeout_ns, &s_ok)) { status = CNV_TIMEOUT; break; }
     }
     if (status == CNV_TIMEOUT) return;
-    // answer -> red/black split layout for the velocity pass
-    {
-        const int ow = t.c1 - t.c0, oh = t.r1 - t.r0;
-        for (int x = threadIdx.x; x < ow * oh; x += kThreads) {
-            const int i = t.r0 + x / ow, j = t.c0 + x % ow;
-            L.sor[(i + j) & 1][(size_t)i * L.pitch + (j >> 1)] = L.psi[(size_t)i * n + j];
-        }
-    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctl->iters = outer;
         ctl->err = rel;
@@ -305,7 +392,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
 cudaError_t launch_mixed(const MixedLaunch& L, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(L.sync, 0, sizeof(MixedSync), s);
     if (e != cudaSuccess) return e;
-    const size_t smem = mixed_smem_bytes(L.n, L.gx, L.gy);
+    const size_t smem = mixed_smem_bytes(L.n, L.gx, L.gy, L.rq_in_smem != 0);
     e = cudaFuncSetAttribute(k_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};

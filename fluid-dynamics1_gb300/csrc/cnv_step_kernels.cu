@@ -111,11 +111,7 @@ __global__ void k_transport(StepArgs a) {
     const double diff = dmul(a.inv_re, dadd(wxx, wyy));
     const double wn = dadd(dmul(dadd(conv, diff), a.dt), w0);
     a.w_out[(size_t)i * n + j] = wn;
-    const bool interior = i > 0 && i < n - 1 && j > 0 && j < n - 1;
-    if (a.g_rowmajor) {
-        // mixed form: c4 * f, row-major, zero on the edge
-        a.g_rowmajor[(size_t)i * n + j] = interior ? dmul(a.c4, -wn) : 0.0;
-    } else if (interior) {
+    if (i > 0 && i < n - 1 && j > 0 && j < n - 1) {
         const int c = (i + j) & 1;
         a.rhs[c][(size_t)i * a.pitch + (j >> 1)] = make_rhs(-wn, a);  // f = -w (invsig)
     }
@@ -223,14 +219,6 @@ __global__ void k_to_split(const double* f, double* r, double* b, StepArgs a) {
     ((i + j) & 1 ? b : r)[(size_t)i * a.pitch + (j >> 1)] = g;
 }
 
-__global__ void k_scale_rhs(const double* f, double* g, int n, double c4) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= n || j >= n) return;
-    const bool interior = i > 0 && i < n - 1 && j > 0 && j < n - 1;
-    g[(size_t)i * n + j] = interior ? dmul(c4, f[(size_t)i * n + j]) : 0.0;
-}
-
 __global__ void k_from_split(const double* r, const double* b, double* f, int n, int pitch) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -276,12 +264,6 @@ cudaError_t launch_continuity(const StepArgs& a, cudaStream_t s) {
 cudaError_t launch_to_split(const double* f, double* r, double* b, const StepArgs& a, cudaStream_t s) {
     const dim3 blk(32, 8);
     k_to_split<<<grid2d(a.n, blk), blk, 0, s>>>(f, r, b, a);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_scale_rhs(const double* f, double* g, int n, double c4, cudaStream_t s) {
-    const dim3 blk(32, 8);
-    k_scale_rhs<<<grid2d(n, blk), blk, 0, s>>>(f, g, n, c4);
     return cudaGetLastError();
 }
 

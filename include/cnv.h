@@ -92,7 +92,7 @@ typedef struct cnv_config {
     int init_smooth_passes;  /* CNV_INIT_NOISE Jacobi averaging passes */
     int device;              /* CUDA device ordinal */
     int solver_blocks;       /* Poisson solver blocks (tiles); <= 0 picks them from the grid size */
-    int mixed_inner_sweeps;  /* CNV_PREC_MIXED: FP32 sweeps per correction; <= 0 picks 2*n */
+    int mixed_inner_sweeps;  /* CNV_PREC_MIXED: FP32 sweeps per correction; <= 0 picks n */
     int mixed_max_outer;     /* CNV_PREC_MIXED: correction limit (CNV_NOT_CONVERGED past it); <= 0: 100 */
     int reserved[5];
 } cnv_config;
