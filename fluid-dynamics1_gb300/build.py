@@ -30,7 +30,8 @@ def _sources():
 
 
 def _headers():
-    return glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(HERE, "..", "include", "*.h"))
+    return (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh"))
+            + glob.glob(os.path.join(HERE, "..", "include", "*.h")))
 
 
 def _compile(src: str, verbose_ptxas: bool) -> tuple[str, str]:

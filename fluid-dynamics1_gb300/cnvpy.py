@@ -50,6 +50,10 @@ class StepInfo(C.Structure):
                 ("cont_max", C.c_double), ("cont_min", C.c_double)]
 
 
+class CavitySpec(C.Structure):
+    _fields_ = [("n", C.c_int), ("Re", C.c_double), ("lid", C.c_double), ("dt", C.c_double)]
+
+
 _dp = C.POINTER(C.c_double)
 _lib = None
 
@@ -78,6 +82,14 @@ _SIGS = {
     "cnv_poisson_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
                                       C.c_int, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), _dp,
                                       C.c_void_p]),
+    "cnv_batch_specs": (C.c_int, [C.c_int, C.c_ulonglong, C.POINTER(CavitySpec)]),
+    "cnv_batch_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(CavitySpec), C.POINTER(C.c_void_p)]),
+    "cnv_batch_destroy": (None, [C.c_void_p]),
+    "cnv_batch_reset": (C.c_int, [C.c_void_p]),
+    "cnv_batch_tune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "cnv_batch_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepInfo)]),
+    "cnv_batch_get_fields": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
+    "cnv_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),
     "cnv_last_error": (C.c_char_p, []),
     "cnv_version": (C.c_char_p, []),
 }
@@ -227,3 +239,69 @@ class Cavity:
 
     def get_fields_device(self, w=0, u=0, v=0, psi=0) -> int:
         return self._lib.cnv_get_fields_device(self._h, w or None, u or None, v or None, psi or None)
+
+
+def batch_specs(count: int, seed: int = 0):
+    """Cavities of the batched workload: n over {64,96,128,192,256,384}, Re in [100,2000], lid in [0.5,1.5]."""
+    arr = (CavitySpec * count)()
+    check(load().cnv_batch_specs(count, seed, arr), "cnv_batch_specs")
+    return [dict(n=a.n, Re=a.Re, lid=a.lid, dt=a.dt) for a in arr]
+
+
+class Batch:
+    """Many cavities advanced by one persistent launch (cnv_batch)."""
+
+    def __init__(self, base: Config, specs):
+        self._lib = load()
+        self.specs = [dict(x) for x in specs]
+        arr = (CavitySpec * len(specs))()
+        for a, x in zip(arr, specs):
+            a.n, a.Re, a.lid, a.dt = x["n"], x["Re"], x["lid"], x.get("dt", 0.0)
+        h = C.c_void_p()
+        check(self._lib.cnv_batch_create(C.byref(base), len(specs), arr, C.byref(h)), "cnv_batch_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.cnv_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def reset(self):
+        check(self._lib.cnv_batch_reset(self._h), "cnv_batch_reset")
+
+    def tune(self):
+        t, b = C.c_int(0), C.c_int(0)
+        check(self._lib.cnv_batch_tune(self._h, C.byref(t), C.byref(b)), "cnv_batch_tune")
+        return t.value, b.value
+
+    def step(self, nsteps: int = 1, raise_on_error: bool = True):
+        info = (StepInfo * len(self.specs))()
+        rc = self._lib.cnv_batch_step(self._h, nsteps, info)
+        if rc != CNV_OK and raise_on_error:
+            raise CnvError(rc, last_error())
+        return rc, [dict(iters=i.iters, status=i.status, err=i.err, cont_max=i.cont_max, cont_min=i.cont_min)
+                    for i in info]
+
+    def get_fields(self, index: int):
+        n = self.specs[index]["n"]
+        w, u, v, psi = (np.empty((n, n)) for _ in range(4))
+        check(self._lib.cnv_batch_get_fields(self._h, index, _ptr(w), _ptr(u), _ptr(v), _ptr(psi)),
+              "cnv_batch_get_fields")
+        return w, u, v, psi
+
+    def stats(self):
+        cells, sweeps, ms = C.c_longlong(0), C.c_longlong(0), C.c_double(0)
+        check(self._lib.cnv_batch_stats(self._h, C.byref(cells), C.byref(sweeps), C.byref(ms)), "cnv_batch_stats")
+        return cells.value, sweeps.value, ms.value

@@ -60,6 +60,8 @@ inline unsigned long long splitmix64(unsigned long long z) {
 
 }  // namespace
 
+void cnv::set_last_error(const char* msg) { g_last_error = msg; }
+
 struct cnv_state {
     cnv_config cfg;
     int n = 0;

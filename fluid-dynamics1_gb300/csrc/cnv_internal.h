@@ -91,4 +91,7 @@ struct PoissonParams {
     long long timeout_ns;  // bound on every wait for another block
 };
 
+// Set the text cnv_last_error() returns on this thread.
+void set_last_error(const char* msg);
+
 }  // namespace cnv

@@ -34,6 +34,7 @@
 #include <cfloat>
 
 #include "cnv_kernels.h"
+#include "cnv_stencil.cuh"
 
 namespace cnv {
 namespace {
@@ -213,10 +214,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
                 const double* po = L.psi[c ^ 1];
                 for (int m = mlo + lane; m <= mhi; m += 32) {
                     const size_t k = (size_t)i * P + m;
-                    const double ap = dy2 * (__ldcg(po + k + P) + __ldcg(po + k - P)) +
-                                      dx2 * (__ldcg(po + k - 1 + q) + __ldcg(po + k + q)) - den * __ldcg(pc + k);
                     const double g = L.g[c][k];
-                    const double R = g - ap;
+                    const double R = poisson_defect(dy2, dx2, den, __ldcg(po + k + P), __ldcg(po + k - P),
+                                                    __ldcg(po + k - 1 + q), __ldcg(po + k + q), __ldcg(pc + k), g);
                     rr = fma(R, R, rr);
                     if (outer == 0) gg = fma(g, g, gg);
                     L.rq[c][k] = (float)(R * L.rden);

@@ -15,52 +15,10 @@
 #include <cfloat>
 
 #include "cnv_kernels.h"
+#include "cnv_stencil.cuh"
 
 namespace cnv {
 namespace {
-
-__device__ __forceinline__ int row_class(int r, int n) { return r < 3 ? r : (r >= n - 3 ? r - n + 7 : 3); }
-
-__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
-
-// Velocity with the Dirichlet values of src/main.c:283-296: the second loop there (columns
-// j = 0 and j = n-1) runs last, so corners take u1/u2 (v1/v2).
-__device__ __forceinline__ double vel_bc(const double* f, int n, int i, int j, double b1, double b2,
-                                         double b3, double b4) {
-    if (j == 0) return b1;
-    if (j == n - 1) return b2;
-    if (i == 0) return b3;
-    if (i == n - 1) return b4;
-    return f[(size_t)i * n + j];
-}
-
-// sum over offsets o of band[class(j)][o] * x(i, j+o), ascending column (DX-type product)
-template <class Load>
-__device__ __forceinline__ double along_j(const double (*band)[kTaps], int n, int i, int j, Load x) {
-    const double* c = band[row_class(j, n)];
-    double acc = 0.0;
-#pragma unroll
-    for (int o = -3; o <= 3; ++o) {
-        const int col = j + o;
-        if (col >= 0 && col < n) acc = dadd(acc, dmul(c[o + 3], x(i, col)));
-    }
-    return acc;
-}
-
-// sum over offsets o of band[class(i)][o] * x(i+o, j), ascending row (DY-type product)
-template <class Load>
-__device__ __forceinline__ double along_i(const double (*band)[kTaps], int n, int i, int j, Load x) {
-    const double* c = band[row_class(i, n)];
-    double acc = 0.0;
-#pragma unroll
-    for (int o = -3; o <= 3; ++o) {
-        const int row = i + o;
-        if (row >= 0 && row < n) acc = dadd(acc, dmul(c[o + 3], x(row, j)));
-    }
-    return acc;
-}
 
 __device__ __forceinline__ double make_rhs(double f_ref, const StepArgs& a) {
     // src/poisson.c:247 multiplies dx*dx*dy*dy*f left to right: (((dx*dx)*dy)*dy)*f = c4*f

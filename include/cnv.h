@@ -177,6 +177,40 @@ int cnv_poisson_noalloc(const double *f, double *psi, int n, double dx, double d
                         int poisson_type, int precision, double beta, int itmax, double tol,
                         int *iters, double *err, void *stream);
 
+/* ---------------------------------------------------------------------------------------
+ * Batched form: many independent cavities (uneven grid size, Re, lid speed) advanced by one
+ * persistent launch (captured in a CUDA graph). Each cavity runs the step of cnv_step with the
+ * mixed-precision Poisson solve (FP32 red-black SOR inside FP64 defect correction to relative
+ * residual base->mixed_rtol, default 1e-10). No counterpart in the reference, which runs one
+ * cavity per process.
+ * ------------------------------------------------------------------------------------- */
+typedef struct cnv_cavity_spec {
+    int n;       /* grid points per side */
+    double Re;   /* Reynolds number */
+    double lid;  /* lid speed (u4) */
+    double dt;   /* time step; <= 0 selects 0.2*min(h^2 Re/4, h/|lid|) */
+} cnv_cavity_spec;
+
+typedef struct cnv_batch cnv_batch;
+
+/* count cavities drawn from a splitmix64 stream: n uniform over {64,96,128,192,256,384},
+ * Re uniform in [100, 2000], lid uniform in [0.5, 1.5], dt by the stability rule. */
+int cnv_batch_specs(int count, unsigned long long seed, cnv_cavity_spec *out);
+/* Fields start as cnv_create's; base supplies order, Lx/Ly, the other wall velocities and the
+ * mixed-form settings. */
+int cnv_batch_create(const cnv_config *base, int count, const cnv_cavity_spec *specs, cnv_batch **out);
+void cnv_batch_destroy(cnv_batch *b);
+int cnv_batch_reset(cnv_batch *b);
+/* Time one step of each candidate launch shape from the initial state, keep the fastest, and
+ * reset the fields. threads / blocks_per_sm may be NULL. */
+int cnv_batch_tune(cnv_batch *b, int *threads, int *blocks_per_sm);
+/* Advance every cavity nsteps steps in one launch; last (count records or NULL) receives each
+ * cavity's last step. */
+int cnv_batch_step(cnv_batch *b, int nsteps, cnv_step_info *last);
+int cnv_batch_get_fields(cnv_batch *b, int index, double *w, double *u, double *v, double *psi);
+/* Total cells, FP32 sweeps of the last call (all cavities) and its device time (ms). */
+int cnv_batch_stats(cnv_batch *b, long long *cells, long long *sweeps, double *ms);
+
 /* Statistics of the last cnv_step/cnv_poisson call: total Poisson sweeps, device time of the
  * whole call (ms, CUDA events on the state's stream) and device time of the Poisson kernel of
  * the last step or solve it ran (ms). Any pointer may be NULL. */

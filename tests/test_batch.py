@@ -1,0 +1,87 @@
+"""Batched form: many cavities of uneven size, Re and lid speed in one persistent launch.
+
+Each cavity must equal a single-cavity run of the same mixed-precision step (same operators,
+same FP32 red-black sweeps, same defect-correction stop rule) to 1e-12 normwise relative per
+field, and match the FP64 oracle run to a tight tolerance within the mixed form's 1e-7.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+SAME_SCHEME_TOL = 1e-12   # batch vs single-cavity mixed run, normwise relative
+ORACLE_TOL = 1e-7         # batch vs FP64 oracle converged tightly, normwise relative
+
+
+def test_specs_generator_is_deterministic_and_in_range(cnv):
+    a = cnv.batch_specs(256, seed=0)
+    b = cnv.batch_specs(256, seed=0)
+    c = cnv.batch_specs(256, seed=1)
+    assert a == b and a != c
+    assert {x["n"] for x in a} == {64, 96, 128, 192, 256, 384}
+    assert all(100 <= x["Re"] <= 2000 and 0.5 <= x["lid"] <= 1.5 for x in a)
+    counts = np.bincount([[64, 96, 128, 192, 256, 384].index(x["n"]) for x in a], minlength=6)
+    assert counts.min() > 20  # roughly uniform over the six sizes
+
+
+def _stable_dt(n, re, lid):
+    h = 1.0 / n
+    return 0.2 * min(h * h * re / 4, h / abs(lid))
+
+
+SPECS = [dict(n=64, Re=400.0, lid=1.0), dict(n=40, Re=1500.0, lid=0.7), dict(n=96, Re=120.0, lid=1.3),
+         dict(n=33, Re=900.0, lid=0.5), dict(n=128, Re=2000.0, lid=1.1)]
+
+
+@pytest.mark.gpu
+def test_batch_equals_single_cavity_runs(cnv):
+    base = cnv.default_config(mixed_rtol=1e-10)
+    nsteps = 3
+    with cnv.Batch(base, SPECS) as bt:
+        rc, last = bt.step(nsteps)
+        fields = [bt.get_fields(k) for k in range(len(SPECS))]
+    assert rc == 0
+    for k, sp in enumerate(SPECS):
+        cfg = cnv.default_config(nx=sp["n"], ny=sp["n"], Re=sp["Re"], u4=sp["lid"],
+                                 dt=_stable_dt(sp["n"], sp["Re"], sp["lid"]), precision=cnv.PREC_MIXED,
+                                 mixed_rtol=1e-10)
+        with cnv.Cavity(cfg) as cav:
+            _, steps = cav.step(nsteps)
+            single = cav.get_fields()
+        assert last[k]["iters"] == steps[-1]["iters"]
+        for name, a, b in zip("w u v psi".split(), fields[k], single):
+            assert np.max(np.abs(a - b)) <= SAME_SCHEME_TOL * np.max(np.abs(b)), (k, name)
+
+
+@pytest.mark.gpu
+def test_batch_matches_fp64_oracle(cnv, orc):
+    base = cnv.default_config(mixed_rtol=1e-10)
+    specs = SPECS[:3]
+    with cnv.Batch(base, specs) as bt:
+        bt.step(3)
+        fields = [bt.get_fields(k) for k in range(len(specs))]
+    for k, sp in enumerate(specs):
+        n = sp["n"]
+        p = orc.make_params(n, re=sp["Re"], dt=_stable_dt(n, sp["Re"], sp["lid"]), u_bc=(0, 0, 0, sp["lid"]),
+                            tol=1e-13 * n * n, itmax=10_000_000, threads=0, exact_norm=0)
+        w, u, v, psi = orc.initial_state(n)
+        orc.run(p, 3, w, u, v, psi)
+        for name, a, b in zip("w u v psi".split(), fields[k], (w, u, v, psi)):
+            assert np.max(np.abs(a - b)) <= ORACLE_TOL * np.max(np.abs(b)), (k, name)
+
+
+@pytest.mark.gpu
+def test_batch_tuned_shape_gives_the_same_fields(cnv):
+    base = cnv.default_config(mixed_rtol=1e-10)
+    specs = cnv.batch_specs(12, seed=3)
+    specs = [dict(x, n=min(x["n"], 128)) for x in specs]  # keep the test quick
+    with cnv.Batch(base, specs) as bt:
+        bt.step(2)
+        ref = [bt.get_fields(k) for k in range(len(specs))]
+        threads, per_sm = bt.tune()
+        assert threads in (256, 512, 1024) and per_sm in (1, 2)
+        bt.step(2)
+        tuned = [bt.get_fields(k) for k in range(len(specs))]
+    for a4, b4 in zip(ref, tuned):
+        for a, b in zip(a4, b4):
+            assert np.max(np.abs(a - b)) <= SAME_SCHEME_TOL * max(np.max(np.abs(b)), 1e-300)
