@@ -16,6 +16,13 @@ cell per sweep: read psi and f, write psi) over its CUDA-event duration, against
 HBM copy bandwidth. cpu_baseline = the CPU oracle (a restatement of the reference's own
 algorithm) on this host's cores for one step of the same workload.
 
+forms = the other ways the library takes the step, each timed the same way and compared field by
+field (max and RMS relative difference) with the plain FP64 path after the same steps:
+fp64_fma and mixed (FP32 sweeps in FP64 defect correction) on the 1024^2 workload; mixed_2048,
+a 2048^2 cavity with a smoothed-noise initial vorticity, mixed against FP64; batched_256, 256
+cavities of uneven size, Re and lid speed in one persistent launch per call against the FP64
+path run cavity by cavity.
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun each rank runs an independent replica (the step does not shard: one cavity per
 GPU); value is the sum over ranks of cells x steps divided by the slowest rank's time.
@@ -203,15 +210,15 @@ FORMS = {
 }
 
 
-def make_config(cnvpy, w, device, precision=0):
+def make_config(cnvpy, w, device, precision=0, **extra):
     return cnvpy.default_config(nx=w["n"], ny=w["n"], Re=w["re"], u4=w["lid"], dt=w["dt"],
                                 poisson_tol=w["tol"], poisson_max_it=w["itmax"], device=device,
-                                precision=precision, mixed_rtol=1e-10)
+                                precision=precision, mixed_rtol=1e-10, **extra)
 
 
-def run_device(cnvpy, w, device, steps, warmup, flush, precision=0, clocks=None):
-    """Device-resident run: returns per-step records with CUDA-event times."""
-    cfg = make_config(cnvpy, w, device, precision)
+def run_device(cnvpy, w, device, steps, warmup, flush, precision=0, clocks=None, fields=False, **extra):
+    """Device-resident run: per-step records with CUDA-event times (and the final fields)."""
+    cfg = make_config(cnvpy, w, device, precision, **extra)
     recs = []
     with cnvpy.Cavity(cfg) as cav:
         for t in range(warmup + steps):
@@ -222,7 +229,99 @@ def run_device(cnvpy, w, device, steps, warmup, flush, precision=0, clocks=None)
             sweeps, ms, pms = cav.stats()
             if t >= warmup:
                 recs.append(dict(ms=ms, poisson_ms=pms, sweeps=sweeps, iters=info[0]["iters"]))
-    return recs
+        out = cav.get_fields() if fields else None
+    return (recs, out) if fields else recs
+
+
+def field_error(test, ref):
+    """Per field (w, u, v, psi): max |test - ref| / max |ref| and RMS(test - ref) / RMS(ref)."""
+    import numpy as np
+
+    out = {}
+    for name, a, b in zip(("w", "u", "v", "psi"), test, ref):
+        d = a - b
+        out[name] = {"max_rel": float(np.max(np.abs(d)) / max(np.max(np.abs(b)), 1e-300)),
+                     "rms_rel": float(np.sqrt(np.mean(d * d)) / max(np.sqrt(np.mean(b * b)), 1e-300))}
+    return out
+
+
+def mcells(cells, steps, ms):
+    return round(cells * steps / (ms * 1e-3) / 1e6, 4)
+
+
+def form_1024(cnvpy, w, local, args, flush, name, ref_fields):
+    """Another precision of the headline workload, with its field error against the FP64 path."""
+    fprec, fdesc = FORMS[name]
+    fr, fields = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=fprec, fields=True)
+    f_ms = sum(r["ms"] for r in fr)
+    return {"value": mcells(w["n"] ** 2, len(fr), f_ms), "unit": UNIT, "steps": len(fr),
+            "sweeps_per_step": sum(r["sweeps"] for r in fr) / len(fr), "solver": fdesc,
+            "error_vs_fp64": field_error(fields, ref_fields),
+            "compared_after_steps": args.warmup + args.steps}
+
+
+def form_mixed_2048(cnvpy, local, flush, steps=3, warmup=3):
+    """2048^2 cavity, Re 1000, initial vorticity = seeded Gaussian noise (sigma 0.1) smoothed by 8
+    Jacobi passes: FP32 sweeps in FP64 defect correction (relative residual 1e-10) against the
+    plain FP64 path (sum|dpsi| < 1e-6), both timed, fields compared after the same steps."""
+    w = workload(2048)
+    init = dict(init_field=1, seed=2024, init_sigma=0.1, init_smooth_passes=8)
+    out = {"workload": f"2048x2048 cavity, Re 1000, lid 1, dt={w['dt']:.6g}, noise initial vorticity "
+                       f"(sigma 0.1, 8 smoothing passes, seed 2024)"}
+    res = {}
+    for name, prec in (("fp64", 0), ("mixed", 2)):
+        fr, fields = run_device(cnvpy, w, local, steps, warmup, flush, precision=prec, fields=True, **init)
+        res[name] = fields
+        out[name] = {"value": mcells(w["n"] ** 2, len(fr), sum(r["ms"] for r in fr)), "unit": UNIT,
+                     "steps": len(fr), "sweeps_per_step": sum(r["sweeps"] for r in fr) / len(fr)}
+    out["mixed"]["error_vs_fp64"] = field_error(res["mixed"], res["fp64"])
+    out["compared_after_steps"] = steps + warmup
+    out["speedup_mixed_over_fp64"] = round(out["mixed"]["value"] / out["fp64"]["value"], 3)
+    return out
+
+
+def form_batched(cnvpy, local, steps, count=256, seed=0):
+    """256 cavities (n from {64,...,384}, Re in [100,2000], lid in [0.5,1.5], stable dt) in one
+    persistent launch per call, shape autotuned; against the plain FP64 path run cavity by
+    cavity on one cavity of each size, fields compared after the same steps."""
+    specs = cnvpy.batch_specs(count, seed=seed)
+    base = cnvpy.default_config(mixed_rtol=1e-10, device=local)
+    out = {"workload": f"{count} cavities, seed {seed}: n uniform over {{64,96,128,192,256,384}}, Re uniform in "
+                       f"[100,2000], lid uniform in [0.5,1.5], dt = 0.2 min(h^2 Re/4, h/lid)"}
+    sample = []
+    for n in sorted({s["n"] for s in specs}):
+        sample.append(next(k for k, s in enumerate(specs) if s["n"] == n))
+    with cnvpy.Batch(base, specs) as bt:
+        threads, per_sm = bt.tune()
+        bt.step(1)
+        rc, last = bt.step(steps)
+        cells, sweeps, ms = bt.stats()
+        fields = {k: bt.get_fields(k) for k in sample}
+    out["batched"] = {"value": mcells(cells, steps, ms), "unit": UNIT, "steps": steps, "cells": cells,
+                      "ms_per_step": round(ms / steps, 3), "tuned_shape": {"threads": threads,
+                                                                           "blocks_per_sm": per_sm},
+                      "max_relative_residual": max(x["err"] for x in last)}
+    f_cells, f_ms, errs = 0, 0.0, {}
+    for k in sample:
+        sp = specs[k]
+        h = 1.0 / sp["n"]
+        dt = sp["dt"] or 0.2 * min(h * h * sp["Re"] / 4.0, h / abs(sp["lid"]))  # the batch's stable dt
+        cfg = cnvpy.default_config(nx=sp["n"], ny=sp["n"], Re=sp["Re"], u4=sp["lid"], dt=dt,
+                                   poisson_tol=1e-6, poisson_max_it=1000000, device=local)
+        with cnvpy.Cavity(cfg) as cav:
+            cav.step(1)
+            cav.step(steps)
+            _, c_ms, _ = cav.stats()
+            errs[f"n{sp['n']}"] = field_error(fields[k], cav.get_fields())
+        f_cells += sp["n"] ** 2
+        f_ms += c_ms
+    out["fp64_cavity_by_cavity"] = {"value": mcells(f_cells, steps, f_ms), "unit": UNIT,
+                                    "sample": "one cavity of each size, each its own cnv_state, one call of "
+                                              f"{steps} steps"}
+    out["batched"]["error_vs_fp64"] = errs
+    out["compared_after_steps"] = steps + 1
+    out["speedup_batched_over_fp64"] = round(out["batched"]["value"] / out["fp64_cavity_by_cavity"]["value"], 3)
+    return out
 
 
 def run_e2e(cnvpy, w, device, steps, warmup):
@@ -286,7 +385,8 @@ def ours(args):
     clocks = ClockSampler(local) if rank == 0 else None
     dist.barrier()
     prec, prec_name = FORMS[args.form]
-    recs = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=prec, clocks=clocks)
+    recs, head_fields = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=prec, clocks=clocks,
+                                   fields=True)
     clk = clocks.stop() if clocks else None
     dist.barrier()
     total_ms = sum(r["ms"] for r in recs)
@@ -318,14 +418,14 @@ def ours(args):
 
     forms = {}
     if not args.skip_forms:
-        for name, (fprec, fdesc) in FORMS.items():
-            if name == args.form:
-                continue
-            fr = run_device(cnvpy, w, local, max(2, args.steps // 4), 1, flush, precision=fprec)
-            f_ms = sum(r["ms"] for r in fr)
-            forms[name] = {"value": round(cells * len(fr) / (f_ms * 1e-3) / 1e6, 4), "unit": UNIT,
-                           "steps": len(fr), "sweeps_per_step": sum(r["sweeps"] for r in fr) / len(fr),
-                           "solver": fdesc}
+        ref_fields = head_fields if args.form == "fp64" else None
+        if ref_fields is None:
+            _, ref_fields = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=0, fields=True)
+        for name in FORMS:
+            if name != args.form and name != "fp64":
+                forms[name] = form_1024(cnvpy, w, local, args, flush, name, ref_fields)
+        forms["mixed_2048"] = form_mixed_2048(cnvpy, local, flush)
+        forms["batched_256"] = form_batched(cnvpy, local, max(5, args.steps // 2))
 
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:

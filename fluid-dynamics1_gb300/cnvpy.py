@@ -17,7 +17,7 @@ CNV_OK, CNV_NOT_CONVERGED, CNV_NONFINITE, CNV_BAD_ARG = 0, 1, 2, 3
 CNV_CUDA_ERROR, CNV_TIMEOUT, CNV_NO_DEVICE, CNV_IO_ERROR = 4, 5, 6, 7
 STATUS_NAMES = {0: "OK", 1: "NOT_CONVERGED", 2: "NONFINITE", 3: "BAD_ARG", 4: "CUDA_ERROR",
                 5: "TIMEOUT", 6: "NO_DEVICE", 7: "IO_ERROR"}
-POISSON_GS, POISSON_SOR, POISSON_JACOBI = 1, 2, 3
+POISSON_GS, POISSON_SOR, POISSON_JACOBI, POISSON_DIRECT = 1, 2, 3, 4
 PREC_FP64, PREC_FP64_FMA, PREC_MIXED = 0, 1, 2
 INIT_REFERENCE, INIT_NOISE = 0, 1
 
@@ -90,6 +90,15 @@ _SIGS = {
     "cnv_batch_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepInfo)]),
     "cnv_batch_get_fields": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
     "cnv_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),
+    "cnv_adjoint_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(C.c_void_p)]),
+    "cnv_adjoint_destroy": (None, [C.c_void_p]),
+    "cnv_adjoint_forward": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_int, _dp]),
+    "cnv_adjoint_backward": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "cnv_adjoint_forward_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p]),
+    "cnv_adjoint_backward_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, _dp]),
+    "cnv_adjoint_enstrophy_gradient": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_int, _dp, _dp, _dp]),
+    "cnv_adjoint_stats": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_longlong)]),
+    "cnv_noise_field": (C.c_int, [C.c_int, C.c_ulonglong, C.c_double, C.c_int, _dp]),
     "cnv_last_error": (C.c_char_p, []),
     "cnv_version": (C.c_char_p, []),
 }
@@ -305,3 +314,81 @@ class Batch:
         cells, sweeps, ms = C.c_longlong(0), C.c_longlong(0), C.c_double(0)
         check(self._lib.cnv_batch_stats(self._h, C.byref(cells), C.byref(sweeps), C.byref(ms)), "cnv_batch_stats")
         return cells.value, sweeps.value, ms.value
+
+
+def noise_field(n: int, seed: int, sigma: float = 1.0, passes: int = 0):
+    """The CNV_INIT_NOISE field: sigma * N(0,1) per cell, then `passes` Jacobi averaging passes."""
+    out = np.empty((n, n))
+    check(load().cnv_noise_field(n, seed, sigma, passes, _ptr(out)), "cnv_noise_field")
+    return out
+
+
+class Adjoint:
+    """Discrete adjoint of the time step (cnv_adjoint): forward runs keep checkpoints every
+    `checkpoint_every` steps; backward returns dJ/dw0 and dJ/dlid for a given dJ/dw(T)."""
+
+    def __init__(self, cfg: Config, checkpoint_every: int = 100):
+        self._lib = load()
+        self.n = cfg.nx
+        self.h2 = (cfg.Lx / cfg.nx) * (cfg.Ly / cfg.ny)
+        self.generation = 0  # counts forward runs (the checkpoints belong to the last one)
+        h = C.c_void_p()
+        check(self._lib.cnv_adjoint_create(C.byref(cfg), checkpoint_every, C.byref(h)), "cnv_adjoint_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.cnv_adjoint_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def forward(self, w0, lid: float, nsteps: int):
+        w0 = np.ascontiguousarray(w0, dtype=np.float64)
+        wT = np.empty_like(w0)
+        check(self._lib.cnv_adjoint_forward(self._h, _ptr(w0), float(lid), nsteps, _ptr(wT)), "cnv_adjoint_forward")
+        self.generation += 1
+        return wT
+
+    def backward(self, g_final):
+        g = np.ascontiguousarray(g_final, dtype=np.float64)
+        gw0 = np.empty_like(g)
+        glid = C.c_double(0)
+        check(self._lib.cnv_adjoint_backward(self._h, _ptr(g), _ptr(gw0), C.byref(glid)), "cnv_adjoint_backward")
+        return gw0, glid.value
+
+    def forward_device(self, w0_ptr: int, lid: float, nsteps: int, wT_ptr: int):
+        check(self._lib.cnv_adjoint_forward_device(self._h, w0_ptr, float(lid), nsteps, wT_ptr),
+              "cnv_adjoint_forward_device")
+        self.generation += 1
+
+    def backward_device(self, g_ptr: int, gw0_ptr: int) -> float:
+        glid = C.c_double(0)
+        check(self._lib.cnv_adjoint_backward_device(self._h, g_ptr, gw0_ptr, C.byref(glid)),
+              "cnv_adjoint_backward_device")
+        return glid.value
+
+    def enstrophy_gradient(self, w0, lid: float, nsteps: int):
+        """J = 1/2 sum w(T)^2 dx dy, dJ/dw0, dJ/dlid."""
+        w0 = np.ascontiguousarray(w0, dtype=np.float64)
+        gw0 = np.empty_like(w0)
+        J, glid = C.c_double(0), C.c_double(0)
+        check(self._lib.cnv_adjoint_enstrophy_gradient(self._h, _ptr(w0), float(lid), nsteps, C.byref(J), _ptr(gw0),
+                                                       C.byref(glid)), "cnv_adjoint_enstrophy_gradient")
+        self.generation += 1
+        return J.value, gw0, glid.value
+
+    def stats(self):
+        f, b, by = C.c_double(0), C.c_double(0), C.c_longlong(0)
+        check(self._lib.cnv_adjoint_stats(self._h, C.byref(f), C.byref(b), C.byref(by)), "cnv_adjoint_stats")
+        return f.value, b.value, by.value

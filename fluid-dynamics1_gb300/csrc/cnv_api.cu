@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "cnv_dst.h"
 #include "cnv_kernels.h"
 
 using namespace cnv;
@@ -58,6 +59,29 @@ inline unsigned long long splitmix64(unsigned long long z) {
     return z ^ (z >> 31);
 }
 
+// w = sigma * N(0,1) per cell (splitmix64 counter stream + Box-Muller), then `passes` Jacobi
+// averaging passes over the interior, edges kept.
+void noise_field(int n, unsigned long long seed, double sigma, int passes, double* w) {
+    const size_t nn = (size_t)n * n;
+    const double two_pi = 6.283185307179586476925286766559;
+    for (size_t k = 0; k < nn; ++k) {
+        const unsigned long long z1 = splitmix64(seed + (2 * k) * 0x9E3779B97F4A7C15ull);
+        const unsigned long long z2 = splitmix64(seed + (2 * k + 1) * 0x9E3779B97F4A7C15ull);
+        const double u1 = ((double)(z1 >> 11) + 0.5) * 0x1.0p-53;
+        const double u2 = (double)(z2 >> 11) * 0x1.0p-53;
+        w[k] = sigma * (std::sqrt(-2.0 * std::log(u1)) * std::cos(two_pi * u2));
+    }
+    std::vector<double> t(nn);
+    for (int pass = 0; pass < passes; ++pass) {
+        t.assign(w, w + nn);
+        for (int i = 1; i < n - 1; ++i)
+            for (int j = 1; j < n - 1; ++j) {
+                const size_t k = (size_t)i * n + j;
+                w[k] = (t[k - n] + t[k + n] + t[k - 1] + t[k + 1]) / 4;
+            }
+    }
+}
+
 }  // namespace
 
 void cnv::set_last_error(const char* msg) { g_last_error = msg; }
@@ -88,6 +112,9 @@ struct cnv_state {
     int mixed_gx = 1, mixed_gy = 1, mixed_epochs = 1, mixed_max_outer = 100;
     bool mixed_rq_smem = false;
     double mixed_rtol = 1e-10;
+    // exact solve by sine transforms (CNV_POISSON_DIRECT)
+    bool direct = false;
+    DstPlan dst{};
     double* cont_partials = nullptr;
     int* flag = nullptr;         // non-finite scan result
     FdBands* bands = nullptr;
@@ -125,6 +152,7 @@ void free_state(cnv_state* s) {
     for (float* b : {s->rq, s->eg})
         if (b) cudaFree(b);
     if (s->msync) cudaFree(s->msync);
+    if (s->direct) dst_plan_destroy(&s->dst);
     if (s->flag) cudaFree(s->flag);
     if (s->sync) cudaFree(s->sync);
     if (s->bands) cudaFree(s->bands);
@@ -143,8 +171,10 @@ int validate(const cnv_config* c) {
         return fail(CNV_BAD_ARG, "** Error: valid orders are 2, 4 or 6 ** (got %d)", c->order);
     if (c->nx < (c->order == 6 ? 5 : 4) || c->nx > 16384)
         return fail(CNV_BAD_ARG, "grid size %d outside [%d, 16384]", c->nx, c->order == 6 ? 5 : 4);
-    if (c->poisson_type < 1 || c->poisson_type > 3)
+    if (c->poisson_type < 1 || c->poisson_type > 4)
         return fail(CNV_BAD_ARG, "Error - invalid option for Poisson solver (%d)", c->poisson_type);
+    if (c->poisson_type == CNV_POISSON_DIRECT && c->precision == CNV_PREC_MIXED)
+        return fail(CNV_BAD_ARG, "the direct Poisson solve is FP64 only (precision %d)", c->precision);
     if (c->precision != CNV_PREC_FP64 && c->precision != CNV_PREC_FP64_FMA && c->precision != CNV_PREC_MIXED)
         return fail(CNV_BAD_ARG, "unknown precision %d", c->precision);
     if (c->Lx <= 0 || c->Ly <= 0 || !(c->Re > 0) || !(c->dt > 0) || c->poisson_max_it < 1 ||
@@ -168,28 +198,8 @@ int upload_initial(cnv_state* s) {
             u[(size_t)i * n + j] = s->cfg.ui;
             v[(size_t)i * n + j] = s->cfg.vi;
         }
-    if (s->cfg.init_field == CNV_INIT_NOISE) {
-        // w = sigma * N(0,1) per cell (splitmix64 counter stream + Box-Muller), then
-        // init_smooth_passes Jacobi averaging passes over the interior, edges kept.
-        const double two_pi = 6.283185307179586476925286766559;
-        const unsigned long long seed = s->cfg.seed;
-        for (size_t k = 0; k < nn; ++k) {
-            const unsigned long long z1 = splitmix64(seed + (2 * k) * 0x9E3779B97F4A7C15ull);
-            const unsigned long long z2 = splitmix64(seed + (2 * k + 1) * 0x9E3779B97F4A7C15ull);
-            const double u1 = ((double)(z1 >> 11) + 0.5) * 0x1.0p-53;
-            const double u2 = (double)(z2 >> 11) * 0x1.0p-53;
-            w[k] = s->cfg.init_sigma * (std::sqrt(-2.0 * std::log(u1)) * std::cos(two_pi * u2));
-        }
-        std::vector<double> t(nn);
-        for (int pass = 0; pass < s->cfg.init_smooth_passes; ++pass) {
-            t = w;
-            for (int i = 1; i < n - 1; ++i)
-                for (int j = 1; j < n - 1; ++j) {
-                    const size_t k = (size_t)i * n + j;
-                    w[k] = (t[k - n] + t[k + n] + t[k - 1] + t[k + 1]) / 4;
-                }
-        }
-    }
+    if (s->cfg.init_field == CNV_INIT_NOISE)
+        noise_field(n, s->cfg.seed, s->cfg.init_sigma, s->cfg.init_smooth_passes, w.data());
     s->cur = 0;
     CNV_CUDA(cudaMemcpyAsync(s->w[0], w.data(), nn * 8, cudaMemcpyHostToDevice, s->stream));
     CNV_CUDA(cudaMemcpyAsync(s->u, u.data(), nn * 8, cudaMemcpyHostToDevice, s->stream));
@@ -273,9 +283,20 @@ MixedLaunch mixed_launch(cnv_state* s) {
 }
 
 // Enqueue the Poisson solve on the split-layout rhs, or on g for the mixed form (psi starts
-// from zero).
-int enqueue_poisson(cnv_state* s) {
+// from zero). The direct solve reads the row-major field `in` scaled by `scale` instead
+// (w with c4 in a step, f with -c4 for a standalone solve) and reports 0 iterations.
+int enqueue_poisson(cnv_state* s, const double* in, double scale) {
     const size_t split_bytes = (size_t)s->n * s->pitch * 8;
+    if (s->direct) {
+        CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
+        CNV_CUDA(cudaMemsetAsync(s->sor[1], 0, split_bytes, s->stream));
+        CNV_CUDA(dst_solve_split(s->dst, in, scale, s->sor[0], s->sor[1], s->pitch, s->stream));
+        // iters, status (int) and err (double) of the control block: 0, CNV_OK, 0.0
+        static_assert(offsetof(Ctrl, status) == offsetof(Ctrl, iters) + 4 && offsetof(Ctrl, err) == offsetof(Ctrl, iters) + 8,
+                      "Ctrl layout");
+        CNV_CUDA(cudaMemsetAsync(reinterpret_cast<char*>(s->ctrl) + offsetof(Ctrl, iters), 0, 16, s->stream));
+        return CNV_OK;
+    }
     if (s->mixed) {
         CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
         CNV_CUDA(cudaMemsetAsync(s->sor[1], 0, split_bytes, s->stream));
@@ -341,7 +362,7 @@ int build_graphs(cnv_state* s) {
 int enqueue_step(cnv_state* s, int parity) {
     CNV_CUDA(cudaGraphLaunch(s->graph[0][parity], s->stream));
     CNV_CUDA(cudaEventRecord(s->evp0, s->stream));
-    int rc = enqueue_poisson(s);
+    int rc = enqueue_poisson(s, s->w[1 - parity], s->sa.c4);
     if (rc != CNV_OK) return rc;
     CNV_CUDA(cudaEventRecord(s->evp1, s->stream));
     CNV_CUDA(cudaGraphLaunch(s->graph[1][parity], s->stream));
@@ -353,6 +374,12 @@ int enqueue_step(cnv_state* s, int parity) {
 extern "C" {
 
 const char* cnv_last_error(void) { return g_last_error.c_str(); }
+
+int cnv_noise_field(int n, unsigned long long seed, double sigma, int passes, double* out) {
+    if (n < 1 || passes < 0 || !out) return fail(CNV_BAD_ARG, "bad noise-field arguments");
+    noise_field(n, seed, sigma, passes, out);
+    return CNV_OK;
+}
 
 const char* cnv_version(void) { return "libcnv 1 (sm_103a, CUDA " CNV_STR(CUDART_VERSION) ")"; }
 
@@ -416,7 +443,8 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     const Arith arith = cfg->precision == CNV_PREC_FP64_FMA ? Arith::kFma : Arith::kExact;
     const bool fold = arith == Arith::kExact && s->dx == s->dy && is_pow2(dx2) && is_pow2(2 * (dx2 + dy2));
     // Poisson solver geometry: co-resident blocks (one tile each), a multiple of the SM count
-    const void* kern = poisson_kernel_ptr(arith, cfg->poisson_type, fold);
+    const void* kern =
+        poisson_kernel_ptr(arith, cfg->poisson_type == CNV_POISSON_DIRECT ? CNV_POISSON_SOR : cfg->poisson_type, fold);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, poisson_threads(), 0) != cudaSuccess ||
         per_sm < 1) {
@@ -473,6 +501,13 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
         }
     }
 #undef ALLOC
+    if (cfg->poisson_type == CNV_POISSON_DIRECT) {
+        s->direct = true;
+        if (dst_plan_create(n, s->dx, s->dy, &s->dst) != CNV_OK) {
+            free_state(s);
+            return fail(CNV_CUDA_ERROR, "sine-transform plan for n = %d", n);
+        }
+    }
     if (cudaMemsetAsync(s->ctrl, 0, sizeof(Ctrl), s->stream) != cudaSuccess ||
         cudaMemsetAsync(s->rhs[0], 0, split * 8, s->stream) != cudaSuccess ||
         cudaMemsetAsync(s->rhs[1], 0, split * 8, s->stream) != cudaSuccess) {
@@ -523,7 +558,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     a.psi = s->psi;
     for (int c = 0; c < 2; ++c) {
         a.sor[c] = s->sor[c];
-        a.rhs[c] = s->rhs[c];
+        a.rhs[c] = s->direct ? nullptr : s->rhs[c];  // the direct solve reads w_out itself
     }
     a.bands = s->bands;
     a.bc = BoundaryValues{cfg->u1, cfg->u2, cfg->u3, cfg->u4, cfg->v1, cfg->v2, cfg->v3, cfg->v4};
@@ -720,7 +755,7 @@ int cnv_poisson_device(cnv_state* s, const double* f, double* psi_out, int* iter
     if (rc != CNV_OK) return rc;
     CNV_CUDA(launch_to_split(f, s->rhs[0], s->rhs[1], s->sa, s->stream));
     CNV_CUDA(cudaEventRecord(s->ev0, s->stream));
-    rc = enqueue_poisson(s);
+    rc = enqueue_poisson(s, f, -s->sa.c4);
     if (rc != CNV_OK) return rc;
     CNV_CUDA(cudaEventRecord(s->ev1, s->stream));
     CNV_CUDA(launch_from_split(s->sor[0], s->sor[1], psi_out, s->n, s->pitch, s->stream));

@@ -18,7 +18,7 @@ struct StepArgs {
     double* v;
     double* psi;               // streamfunction, row-major (output copy)
     double* sor[2];            // psi, red/black split layout
-    double* rhs[2];            // Poisson right-hand side, split layout
+    double* rhs[2];            // Poisson right-hand side, split layout (null: not written)
     const FdBands* bands;      // device copy of the operator bands
     BoundaryValues bc;
     double inv_re;             // 1. / Re as src/fluiddyn.c:98 evaluates it

@@ -69,7 +69,7 @@ __global__ void k_transport(StepArgs a) {
     const double diff = dmul(a.inv_re, dadd(wxx, wyy));
     const double wn = dadd(dmul(dadd(conv, diff), a.dt), w0);
     a.w_out[(size_t)i * n + j] = wn;
-    if (i > 0 && i < n - 1 && j > 0 && j < n - 1) {
+    if (a.rhs[0] && i > 0 && i < n - 1 && j > 0 && j < n - 1) {  // no rhs: direct solve reads w_out
         const int c = (i + j) & 1;
         a.rhs[c][(size_t)i * a.pitch + (j >> 1)] = make_rhs(-wn, a);  // f = -w (invsig)
     }

@@ -41,7 +41,10 @@ typedef enum cnv_status {
 enum {
     CNV_POISSON_GS = 1,     /* "no relaxation" (src/poisson.c:62-109), run as red-black GS */
     CNV_POISSON_SOR = 2,    /* SOR (src/poisson.c:111-173), red-black ordering */
-    CNV_POISSON_JACOBI = 3  /* true Jacobi sweeps (extension; src/cuda_kernels.cu:229-246) */
+    CNV_POISSON_JACOBI = 3, /* true Jacobi sweeps (extension; src/cuda_kernels.cu:229-246) */
+    CNV_POISSON_DIRECT = 4  /* extension: exact solve of the same discrete equation by FP64 sine
+                               transforms (the answer SOR converges to, to rounding); iters and
+                               err of the step records are 0; FP64 precisions only */
 };
 
 /* Arithmetic of the Poisson sweeps (extension key "precision"). */
@@ -211,10 +214,44 @@ int cnv_batch_get_fields(cnv_batch *b, int index, double *w, double *u, double *
 /* Total cells, FP32 sweeps of the last call (all cavities) and its device time (ms). */
 int cnv_batch_stats(cnv_batch *b, long long *cells, long long *sweeps, double *ms);
 
+/* ---------------------------------------------------------------------------------------
+ * Differentiable form: the discrete adjoint of the time step. A cnv_adjoint advances one
+ * cavity with the step of cnv_step (the same wall, transport and velocity passes) and the
+ * exact Poisson solve of CNV_POISSON_DIRECT, and returns the gradient of a scalar of the final
+ * vorticity with respect to the initial vorticity and the lid speed (u4) by hand-written adjoint
+ * kernels. The forward run keeps a checkpoint of the state every checkpoint_every steps; the
+ * backward run recomputes one segment at a time from its checkpoint. The initial velocities
+ * are cfg's ui, vi on the interior (src/main.c:213-221); cfg's poisson_* and precision fields
+ * are not used. No counterpart in the reference.
+ * ------------------------------------------------------------------------------------- */
+typedef struct cnv_adjoint cnv_adjoint;
+
+int cnv_adjoint_create(const cnv_config *cfg, int checkpoint_every, cnv_adjoint **out);
+void cnv_adjoint_destroy(cnv_adjoint *a);
+/* nsteps steps from the initial vorticity w0 (n*n, row-major) with lid speed lid; the final
+ * vorticity goes to w_final (may be NULL). Keeps the checkpoints for cnv_adjoint_backward. */
+int cnv_adjoint_forward(cnv_adjoint *a, const double *w0, double lid, int nsteps, double *w_final);
+/* Given g_final = dJ/dw(T) (n*n) for the last forward run, writes dJ/dw0 (n*n; zero on the
+ * edges, which the first wall pass overwrites) and dJ/dlid (may be NULL). */
+int cnv_adjoint_backward(cnv_adjoint *a, const double *g_final, double *g_w0, double *g_lid);
+/* The same two calls on device pointers (the handle's stream; both return after it is idle). */
+int cnv_adjoint_forward_device(cnv_adjoint *a, const double *w0, double lid, int nsteps, double *w_final);
+int cnv_adjoint_backward_device(cnv_adjoint *a, const double *g_final, double *g_w0, double *g_lid);
+/* J = 1/2 sum over all cells of w(T)^2 dx dy (the final enstrophy) and its gradient. */
+int cnv_adjoint_enstrophy_gradient(cnv_adjoint *a, const double *w0, double lid, int nsteps, double *J,
+                                   double *g_w0, double *g_lid);
+/* Device time (ms) of the last forward and backward runs, and bytes of checkpoint and segment
+ * state held. Any pointer may be NULL. */
+int cnv_adjoint_stats(cnv_adjoint *a, double *forward_ms, double *backward_ms, long long *state_bytes);
+
 /* Statistics of the last cnv_step/cnv_poisson call: total Poisson sweeps, device time of the
  * whole call (ms, CUDA events on the state's stream) and device time of the Poisson kernel of
  * the last step or solve it ran (ms). Any pointer may be NULL. */
 int cnv_last_stats(cnv_state *s, long long *sweeps, double *ms, double *poisson_ms);
+
+/* The CNV_INIT_NOISE initial vorticity as a host array (n*n): sigma * N(0,1) per cell from a
+ * splitmix64 stream seeded with seed, then `passes` Jacobi averaging passes over the interior. */
+int cnv_noise_field(int n, unsigned long long seed, double sigma, int passes, double *out);
 
 /* Human-readable text for the last failing call on this thread. */
 const char *cnv_last_error(void);

@@ -80,7 +80,7 @@ def test_missing_config_file_keeps_defaults(cnv, tmp_path):
     assert c.nx == 64 and c.Re == 1000.0
 
 
-@pytest.mark.parametrize("field,value", [("ny", 63), ("order", 3), ("poisson_type", 4), ("nx", 3),
+@pytest.mark.parametrize("field,value", [("ny", 63), ("order", 3), ("poisson_type", 5), ("nx", 3),
                                          ("precision", 9), ("dt", 0.0), ("u1", 1e6)])
 def test_create_rejects_bad_arguments_without_touching_the_gpu(cnv, field, value):
     cfg = cnv.default_config()
