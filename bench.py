@@ -17,11 +17,13 @@ HBM copy bandwidth. cpu_baseline = the CPU oracle (a restatement of the referenc
 algorithm) on this host's cores for one step of the same workload.
 
 forms = the other ways the library takes the step, each timed the same way and compared field by
-field (max and RMS relative difference) with the plain FP64 path after the same steps:
-fp64_fma and mixed (FP32 sweeps in FP64 defect correction) on the 1024^2 workload; mixed_2048,
-a 2048^2 cavity with a smoothed-noise initial vorticity, mixed against FP64; batched_256, 256
-cavities of uneven size, Re and lid speed in one persistent launch per call against the FP64
-path run cavity by cavity.
+field (max and RMS relative difference) after the same steps with the plain FP64 SOR path and
+with the converged FP64 answer (the direct sine-transform solve): fp64_fma, mixed (FP32 sweeps
+in FP64 defect correction) and direct on the 1024^2 workload; mixed_2048, a 2048^2 cavity with
+a smoothed-noise initial vorticity; batched_256, 256 cavities of uneven size, Re and lid speed
+in one persistent launch per call against the FP64 path run cavity by cavity; adjoint_256, the
+gradient of the final enstrophy of a 256^2 cavity after 2000 steps with respect to the initial
+vorticity and the lid speed, checked against central differences on 16 random directions.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun each rank runs an independent replica (the step does not shard: one cavity per
@@ -201,24 +203,68 @@ def profiled_traffic_per_launch():
     return None
 
 
+def form_adjoint(cnvpy, local, ndirs=16, n=256, steps=2000, every=100, eps=1e-6):
+    """256^2 cavity, Re 400, 2000 steps, initial vorticity = seeded smooth Gaussian field: gradient
+    of J = 1/2 sum w(T)^2 h^2 with respect to w0 and the lid speed by the adjoint kernels
+    (checkpoints every 100 steps), checked against central differences on seeded random
+    directions; cost of forward and gradient."""
+    import numpy as np
+
+    h = 1.0 / n
+    dt = 0.2 * min(h * h * 400.0 / 4, h)
+    cfg = cnvpy.default_config(nx=n, ny=n, Re=400.0, dt=dt, device=local)
+    w0 = cnvpy.noise_field(n, seed=2025, sigma=1.0, passes=16)
+    rng = np.random.default_rng(2026)
+    with cnvpy.Adjoint(cfg, every) as adj:
+        adj.enstrophy_gradient(w0, 1.0, steps)  # warm-up
+        J, gw, glid = adj.enstrophy_gradient(w0, 1.0, steps)
+        fwd_ms, bwd_ms, state_bytes = adj.stats()
+
+        def objective(w, l):
+            wT = adj.forward(w, l, steps)
+            return 0.5 * adj.h2 * float(np.sum(wT * wT))
+
+        errs = []
+        for _ in range(ndirs):
+            d = np.zeros((n, n))
+            d[1:-1, 1:-1] = rng.standard_normal((n - 2, n - 2))
+            dl = float(rng.standard_normal())
+            fd = (objective(w0 + eps * d, 1.0 + eps * dl) - objective(w0 - eps * d, 1.0 - eps * dl)) / (2 * eps)
+            ad = float(np.sum(gw * d)) + glid * dl
+            errs.append(abs(fd - ad) / abs(ad))
+        fwd_only_ms = adj.stats()[0]
+    return {"workload": f"{n}x{n} cavity, Re 400, lid 1, dt={dt:.6g}, {steps} steps, initial vorticity = seeded "
+                        f"Gaussian noise (sigma 1, seed 2025) smoothed by 16 Jacobi passes; J = 1/2 sum w(T)^2 h^2",
+            "J": J, "dJ_dlid": glid, "grad_w0_norm": float(np.linalg.norm(gw)),
+            "forward_ms": round(fwd_only_ms, 2), "gradient_ms": round(fwd_ms + bwd_ms, 2),
+            "gradient_cost_over_forward": round((fwd_ms + bwd_ms) / fwd_only_ms, 3),
+            "forward_value": mcells(n * n, steps, fwd_only_ms), "unit": UNIT,
+            "checkpoint_every": every, "state_bytes": state_bytes,
+            "fd_check": {"directions": ndirs, "eps": eps, "max_rel_err": max(errs),
+                         "median_rel_err": float(np.median(errs))},
+            "poisson": "direct (exact sine-transform solve; self-adjoint)"}
+
+
 # ------------------------------------------------------------------------------- our arm
 FORMS = {
-    # name: (precision, description)
-    "fp64": (0, "fp64 (reference rounding)"),
-    "fp64_fma": (1, "fp64 (FMA form of the SOR update)"),
-    "mixed": (2, "FP32 red-black SOR sweeps inside FP64 defect correction to relative residual 1e-10"),
+    # name: (precision, poisson_type, description)
+    "fp64": (0, 2, "fp64 red-black SOR, reference rounding"),
+    "fp64_fma": (1, 2, "fp64 red-black SOR, FMA form of the update"),
+    "mixed": (2, 2, "FP32 red-black SOR sweeps inside FP64 defect correction to relative residual 1e-10"),
+    "direct": (0, 4, "exact FP64 sine-transform solve of the same discrete equation (converged answer)"),
 }
 
 
-def make_config(cnvpy, w, device, precision=0, **extra):
+def make_config(cnvpy, w, device, precision=0, poisson_type=2, **extra):
     return cnvpy.default_config(nx=w["n"], ny=w["n"], Re=w["re"], u4=w["lid"], dt=w["dt"],
                                 poisson_tol=w["tol"], poisson_max_it=w["itmax"], device=device,
-                                precision=precision, mixed_rtol=1e-10, **extra)
+                                precision=precision, poisson_type=poisson_type, mixed_rtol=1e-10, **extra)
 
 
-def run_device(cnvpy, w, device, steps, warmup, flush, precision=0, clocks=None, fields=False, **extra):
+def run_device(cnvpy, w, device, steps, warmup, flush, precision=0, poisson_type=2, clocks=None, fields=False,
+               **extra):
     """Device-resident run: per-step records with CUDA-event times (and the final fields)."""
-    cfg = make_config(cnvpy, w, device, precision, **extra)
+    cfg = make_config(cnvpy, w, device, precision, poisson_type, **extra)
     recs = []
     with cnvpy.Cavity(cfg) as cav:
         for t in range(warmup + steps):
@@ -249,34 +295,45 @@ def mcells(cells, steps, ms):
     return round(cells * steps / (ms * 1e-3) / 1e6, 4)
 
 
-def form_1024(cnvpy, w, local, args, flush, name, ref_fields):
-    """Another precision of the headline workload, with its field error against the FP64 path."""
-    fprec, fdesc = FORMS[name]
-    fr, fields = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=fprec, fields=True)
+def form_1024(cnvpy, w, local, args, flush, name, ref_fields, conv_fields):
+    """Another solver of the headline workload, with its field errors against the FP64 SOR path
+    and against the converged FP64 answer (the direct solve)."""
+    fprec, ptype, fdesc = FORMS[name]
+    fr, fields = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=fprec, poisson_type=ptype,
+                            fields=True)
     f_ms = sum(r["ms"] for r in fr)
-    return {"value": mcells(w["n"] ** 2, len(fr), f_ms), "unit": UNIT, "steps": len(fr),
-            "sweeps_per_step": sum(r["sweeps"] for r in fr) / len(fr), "solver": fdesc,
-            "error_vs_fp64": field_error(fields, ref_fields),
-            "compared_after_steps": args.warmup + args.steps}
+    out = {"value": mcells(w["n"] ** 2, len(fr), f_ms), "unit": UNIT, "steps": len(fr),
+           "sweeps_per_step": sum(r["sweeps"] for r in fr) / len(fr), "solver": fdesc,
+           "compared_after_steps": args.warmup + args.steps}
+    if ref_fields is not None:
+        out["error_vs_fp64_sor"] = field_error(fields, ref_fields)
+    if conv_fields is not None and name != "direct":
+        out["error_vs_converged_fp64"] = field_error(fields, conv_fields)
+    return out, fields
 
 
 def form_mixed_2048(cnvpy, local, flush, steps=3, warmup=3):
     """2048^2 cavity, Re 1000, initial vorticity = seeded Gaussian noise (sigma 0.1) smoothed by 8
     Jacobi passes: FP32 sweeps in FP64 defect correction (relative residual 1e-10) against the
-    plain FP64 path (sum|dpsi| < 1e-6), both timed, fields compared after the same steps."""
+    plain FP64 path (sum|dpsi| < 1e-6) and the direct solve, all timed; fields compared with the
+    converged FP64 answer (the direct solve) after the same steps."""
     w = workload(2048)
     init = dict(init_field=1, seed=2024, init_sigma=0.1, init_smooth_passes=8)
     out = {"workload": f"2048x2048 cavity, Re 1000, lid 1, dt={w['dt']:.6g}, noise initial vorticity "
                        f"(sigma 0.1, 8 smoothing passes, seed 2024)"}
     res = {}
-    for name, prec in (("fp64", 0), ("mixed", 2)):
-        fr, fields = run_device(cnvpy, w, local, steps, warmup, flush, precision=prec, fields=True, **init)
+    for name, prec, ptype in (("fp64", 0, 2), ("mixed", 2, 2), ("direct", 0, 4)):
+        fr, fields = run_device(cnvpy, w, local, steps, warmup, flush, precision=prec, poisson_type=ptype, fields=True,
+                                **init)
         res[name] = fields
         out[name] = {"value": mcells(w["n"] ** 2, len(fr), sum(r["ms"] for r in fr)), "unit": UNIT,
                      "steps": len(fr), "sweeps_per_step": sum(r["sweeps"] for r in fr) / len(fr)}
-    out["mixed"]["error_vs_fp64"] = field_error(res["mixed"], res["fp64"])
+    for name in ("fp64", "mixed"):
+        out[name]["error_vs_converged_fp64"] = field_error(res[name], res["direct"])
+    out["mixed"]["error_vs_fp64_sor"] = field_error(res["mixed"], res["fp64"])
     out["compared_after_steps"] = steps + warmup
     out["speedup_mixed_over_fp64"] = round(out["mixed"]["value"] / out["fp64"]["value"], 3)
+    out["speedup_direct_over_fp64"] = round(out["direct"]["value"] / out["fp64"]["value"], 3)
     return out
 
 
@@ -312,13 +369,19 @@ def form_batched(cnvpy, local, steps, count=256, seed=0):
             cav.step(1)
             cav.step(steps)
             _, c_ms, _ = cav.stats()
-            errs[f"n{sp['n']}"] = field_error(fields[k], cav.get_fields())
+            sor_fields = cav.get_fields()
+        cfg.poisson_type = 4
+        with cnvpy.Cavity(cfg) as cav:
+            cav.step(1 + steps)
+            conv = cav.get_fields()
+        errs[f"n{sp['n']}"] = {"batched_vs_converged_fp64": field_error(fields[k], conv),
+                               "fp64_sor_vs_converged_fp64": field_error(sor_fields, conv)}
         f_cells += sp["n"] ** 2
         f_ms += c_ms
     out["fp64_cavity_by_cavity"] = {"value": mcells(f_cells, steps, f_ms), "unit": UNIT,
                                     "sample": "one cavity of each size, each its own cnv_state, one call of "
                                               f"{steps} steps"}
-    out["batched"]["error_vs_fp64"] = errs
+    out["errors"] = errs
     out["compared_after_steps"] = steps + 1
     out["speedup_batched_over_fp64"] = round(out["batched"]["value"] / out["fp64_cavity_by_cavity"]["value"], 3)
     return out
@@ -384,9 +447,9 @@ def ours(args):
     flush = L2Flusher(local)
     clocks = ClockSampler(local) if rank == 0 else None
     dist.barrier()
-    prec, prec_name = FORMS[args.form]
-    recs, head_fields = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=prec, clocks=clocks,
-                                   fields=True)
+    prec, ptype, prec_name = FORMS[args.form]
+    recs, head_fields = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=prec,
+                                   poisson_type=ptype, clocks=clocks, fields=True)
     clk = clocks.stop() if clocks else None
     dist.barrier()
     total_ms = sum(r["ms"] for r in recs)
@@ -417,15 +480,23 @@ def ours(args):
            "host_buffers": "pinned" if pinned else "pageable"}
 
     forms = {}
+    conv_err = None
     if not args.skip_forms:
-        ref_fields = head_fields if args.form == "fp64" else None
-        if ref_fields is None:
-            _, ref_fields = run_device(cnvpy, w, local, args.steps, args.warmup, flush, precision=0, fields=True)
+        # converged FP64 answer of the same steps (direct solve), and the FP64 SOR path's fields
+        direct_form, conv_fields = form_1024(cnvpy, w, local, args, flush, "direct",
+                                             head_fields if args.form == "fp64" else None, None)
+        sor_fields = head_fields
+        if args.form != "fp64":
+            _, sor_fields = run_device(cnvpy, w, local, args.steps, args.warmup, flush, fields=True)
+            direct_form["error_vs_fp64_sor"] = field_error(conv_fields, sor_fields)
+        conv_err = field_error(head_fields, conv_fields)
         for name in FORMS:
-            if name != args.form and name != "fp64":
-                forms[name] = form_1024(cnvpy, w, local, args, flush, name, ref_fields)
+            if name not in (args.form, "fp64", "direct"):
+                forms[name], _ = form_1024(cnvpy, w, local, args, flush, name, sor_fields, conv_fields)
+        forms["direct"] = direct_form
         forms["mixed_2048"] = form_mixed_2048(cnvpy, local, flush)
         forms["batched_256"] = form_batched(cnvpy, local, max(5, args.steps // 2))
+        forms["adjoint_256"] = form_adjoint(cnvpy, local)
 
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:
@@ -448,6 +519,8 @@ def ours(args):
         "clocks": clk,
         "forms": forms,
     }
+    if conv_err is not None:
+        line["error_vs_converged_fp64"] = conv_err
     if cpu:
         line["cpu_baseline"] = cpu
     if rank == 0:
@@ -503,7 +576,8 @@ def main():
     ap.add_argument("--n", type=int, default=1024, help=argparse.SUPPRESS)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--skip-forms", action="store_true", help="omit the extra precision/batch forms")
-    ap.add_argument("--form", choices=sorted(FORMS), default="fp64", help="form measured for the headline value")
+    ap.add_argument("--form", choices=["fp64", "fp64_fma", "mixed"], default="fp64",
+                    help="form measured for the headline value")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least 3 untimed warm-up steps
     if args.impl == "reference":

@@ -6,6 +6,11 @@ host-side constants (dx*dx*dy*dy, 2*(dx*dx+dy*dy), ...) round exactly as the ref
 every host, aarch64 included. Device code that must match the reference bit for bit uses the
 round-to-nearest intrinsics, which nvcc never contracts.
 
+Then the two host-only pieces on top of libcnv, with gcc:
+    libcnv_compat.so   the reference's poisson*/euler entry points (compat/cnv_compat.c)
+    cnavier_gpu        the reference program's command line and outputs (app/cnavier_gpu.c)
+both linked against libcnv.so with rpath $ORIGIN.
+
     python fluid-dynamics1_gb300/build.py [--verbose-ptxas] [--force]
 """
 from __future__ import annotations
@@ -20,6 +25,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcnv.so")
+COMPAT_LIB = os.path.join(HERE, "libcnv_compat.so")
+APP = os.path.join(HERE, "cnavier_gpu")
+CC = os.environ.get("CC", "gcc")
+CFLAGS = ["-O2", "-std=gnu99", "-fPIC", "-ffp-contract=off", "-I", os.path.join(HERE, "..", "include")]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", os.path.join(HERE, "..", "include")]
@@ -47,8 +56,30 @@ def _compile(src: str, verbose_ptxas: bool) -> tuple[str, str]:
     return obj, r.stderr
 
 
+def _host_parts(force: bool) -> None:
+    """libcnv_compat.so and cnavier_gpu (gcc, linked against libcnv.so)."""
+    link = ["-L", HERE, "-lcnv", "-Wl,-rpath,$ORIGIN", "-lm", "-lpthread"]
+    jobs = [(os.path.join(HERE, "compat", "cnv_compat.c"), COMPAT_LIB, ["-shared"]),
+            (os.path.join(HERE, "app", "cnavier_gpu.c"), APP, [])]
+    for src, out, extra in jobs:
+        newest = max(os.path.getmtime(p) for p in [src, LIB, __file__] + _headers())
+        if not force and os.path.exists(out) and os.path.getmtime(out) >= newest:
+            continue
+        tmp = out + ".tmp"
+        r = subprocess.run([CC, *CFLAGS, *extra, src, "-o", tmp, *link], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"gcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, out)
+
+
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     """Compile (if stale) and return the path of libcnv.so."""
+    _build_lib(force, verbose_ptxas)
+    _host_parts(force)
+    return LIB
+
+
+def _build_lib(force: bool, verbose_ptxas: bool) -> str:
     os.makedirs(BUILD, exist_ok=True)
     srcs = _sources()
     newest_input = max(os.path.getmtime(p) for p in srcs + _headers() + [__file__])

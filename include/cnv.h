@@ -249,6 +249,32 @@ int cnv_adjoint_stats(cnv_adjoint *a, double *forward_ms, double *backward_ms, l
  * the last step or solve it ran (ms). Any pointer may be NULL. */
 int cnv_last_stats(cnv_state *s, long long *sweeps, double *ms, double *poisson_ms);
 
+/* ---------------------------------------------------------------------------------------
+ * Pieces of the step for callers that keep the reference's loop: the Euler update of
+ * src/fluiddyn.c:71-102 from caller-supplied derivative fields (count points, in place on w,
+ * bit-identical to the reference), on host arrays (staged through per-thread device buffers)
+ * or device arrays (enqueued on stream).
+ * ------------------------------------------------------------------------------------- */
+int cnv_euler(double *w, const double *dwdx, const double *dwdy, const double *d2wdx2, const double *d2wdy2,
+              const double *u, const double *v, long long count, double Re, double dt);
+int cnv_euler_device(double *w, const double *dwdx, const double *dwdy, const double *d2wdx2,
+                     const double *d2wdy2, const double *u, const double *v, long long count, double Re,
+                     double dt, void *stream);
+
+/* ---------------------------------------------------------------------------------------
+ * Run outputs in the reference's formats.
+ * cnv_format_step_log: the lines the reference logs for time step t (src/poisson.c:275 and
+ * src/main.c:401-414) from its step record: the Poisson line, then "Iteration: ... | Time: ...
+ * | Progress: ... | Iter time: ..." and "Continuity max: ... | Continuity min: ... | Elapsed:
+ * ... | Est. remaining: ..." (timings from the caller; it_max as src/main.c:162 computes it).
+ * For a step that did not converge, the reference's error line alone. NUL-terminated into buf.
+ * cnv_write_vtk: src/utils.c:38-99 -- "<output_dir>/<title>-1-<count>.vtk", ASCII
+ * STRUCTURED_POINTS, "%.6lf" values, one line per row, appended; creates output_dir.
+ * ------------------------------------------------------------------------------------- */
+int cnv_format_step_log(const cnv_step_info *info, int t, double dt, int it_max, double iter_seconds,
+                        double elapsed_seconds, char *buf, size_t len);
+int cnv_write_vtk(const char *output_dir, const char *title, int count, const double *field, int m, int n);
+
 /* The CNV_INIT_NOISE initial vorticity as a host array (n*n): sigma * N(0,1) per cell from a
  * splitmix64 stream seeded with seed, then `passes` Jacobi averaging passes over the interior. */
 int cnv_noise_field(int n, unsigned long long seed, double sigma, int passes, double *out);

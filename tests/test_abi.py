@@ -10,10 +10,14 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
+# header -> the library that must export its functions
+LIBRARIES = {"cnv.h": "libcnv.so", "cnv_compat.h": "libcnv_compat.so"}
+
+
+def declared_symbols(header=None):
     names = set()
     for h in os.listdir(os.path.join(ROOT, "include")):
-        if not h.endswith(".h"):
+        if not h.endswith(".h") or (header and h != header):
             continue
         text = open(os.path.join(ROOT, "include", h)).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
@@ -25,13 +29,31 @@ def declared_symbols():
     return names
 
 
-def test_library_exports_every_declared_symbol(cnv):
+def test_every_header_is_mapped_to_a_library():
+    headers = {h for h in os.listdir(os.path.join(ROOT, "include")) if h.endswith(".h")}
+    assert headers == set(LIBRARIES)
+
+
+@pytest.mark.parametrize("header", sorted(LIBRARIES))
+def test_library_exports_every_declared_symbol(cnv, header):
     import ctypes
 
-    lib = ctypes.CDLL(cnv.LIB_PATH)
-    missing = [s for s in sorted(declared_symbols()) if not hasattr(lib, s)]
-    assert not missing, missing
-    assert "cnv_step" in declared_symbols()
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(cnv.LIB_PATH), LIBRARIES[header]))
+    declared = declared_symbols(header)
+    missing = [s for s in sorted(declared) if not hasattr(lib, s)]
+    assert declared and not missing, missing
+
+
+def test_compat_library_mirrors_reference_signatures():
+    # the reference's call shapes (include/poisson.h:10-15, include/fluiddyn.h:5-7, :10)
+    text = open(os.path.join(ROOT, "include", "cnv_compat.h")).read()
+    for decl in ["mtrx poisson(mtrx f, double dx, double dy, int itmax, double tol);",
+                 "mtrx poisson_SOR(mtrx f, double dx, double dy, int itmax, double tol, double beta);",
+                 "mtrx poisson_log(mtrx f, double dx, double dy, int itmax, double tol, FILE *log_file);",
+                 "mtrx poisson_SOR_log(mtrx f, double dx, double dy, int itmax, double tol, double beta, FILE *log_file);",
+                 "void euler(mtrx w, mtrx dwdx, mtrx dwdy, mtrx d2wdx2, mtrx d2wdy2, mtrx u, mtrx v, double Re, double dt);",
+                 "mtrx continuity(mtrx dudx, mtrx dvdy);", "double error(mtrx u1, mtrx u2);"]:
+        assert decl in text, decl
 
 
 def test_config_defaults_match_reference(cnv):
