@@ -567,6 +567,33 @@ def reference(args):
     print(json.dumps(line), flush=True)
 
 
+def only(args):
+    """One small invocation of each named form, in order, for profilers: the kernels run as in the
+    forms above; prints one JSON line of wall times (not a benchmark result)."""
+    import cnvpy
+
+    cnvpy.load()
+    out = {}
+    for name in args.only.split(","):
+        t0 = time.perf_counter()
+        if name in ("fp64", "fp64_fma", "mixed", "direct"):
+            prec, ptype, _ = FORMS[name]
+            run_device(cnvpy, workload(1024), 0, 1, 0, lambda: None, precision=prec, poisson_type=ptype)
+        elif name == "batched":
+            with cnvpy.Batch(cnvpy.default_config(mixed_rtol=1e-10), cnvpy.batch_specs(256, seed=0)) as bt:
+                bt.step(1)
+        elif name == "adjoint":
+            n = 256
+            h = 1.0 / n
+            cfg = cnvpy.default_config(nx=n, ny=n, Re=400.0, dt=0.2 * min(h * h * 100.0, h))
+            with cnvpy.Adjoint(cfg, 10) as adj:
+                adj.enstrophy_gradient(cnvpy.noise_field(n, seed=2025, sigma=1.0, passes=16), 1.0, 20)
+        else:
+            raise SystemExit(f"unknown form {name}")
+        out[name] = round(time.perf_counter() - t0, 3)
+    print(json.dumps({"only": out, "unit": "s (wall, first call)"}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -578,9 +605,14 @@ def main():
     ap.add_argument("--skip-forms", action="store_true", help="omit the extra precision/batch forms")
     ap.add_argument("--form", choices=["fp64", "fp64_fma", "mixed"], default="fp64",
                     help="form measured for the headline value")
+    ap.add_argument("--only", default=None,
+                    help="comma list of fp64,fp64_fma,mixed,direct,batched,adjoint: run one small case of each "
+                         "(for profilers) and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least 3 untimed warm-up steps
-    if args.impl == "reference":
+    if args.only:
+        only(args)
+    elif args.impl == "reference":
         reference(args)
     else:
         ours(args)

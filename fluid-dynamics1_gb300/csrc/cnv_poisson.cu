@@ -30,9 +30,9 @@
 //     new = RN(RN(beta/4 * RN(RN(RN(up+dn) + RN(rt+lt)) - g')) + RN((1-beta)*old))
 // with g' = c4*f / dx^2, which equals the reference's value whenever no intermediate
 // (up+dn, rt+lt, their sum, sum - g') lies below 2^-960 in magnitude (then every power-of-two
-// scaling is exact); cells that fail that test use the full sequence. 9 FP64 operations instead
-// of 12. Arith::kFma uses the FMA form  new = old + beta*(wy*(up+dn) + wx*(rt+lt) - q - old)
-// with q = c4*f/den: 7 FP64 operations.
+// scaling is exact); cells that fail that test use the full sequence. 7 FP64 operations instead
+// of 10 (c4*f comes precomputed from the transport pass in both). Arith::kFma uses the FMA form
+// new = old + beta*(wy*(up+dn) + wx*(rt+lt) - q - old) with q = c4*f/den: 7 FP64 operations.
 #include <algorithm>
 #include <cfloat>
 

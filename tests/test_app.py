@@ -108,8 +108,8 @@ def test_program_reproduces_shipped_redblack_logs(tmp_path, run):
     golden = json.load(open(GOLDEN))[run]
     steps = len(golden["steps"])
     dt = golden["dt"]
-    # tf = (steps + 1) * dt gives it_max + 1 = steps steps (src/main.c:162)
-    cfg = CONFIGS[run] + f"tf = {(steps + 1) * dt!r}\noutput_interval = 1000000\n"
+    # the extension key nsteps fixes the step count (tf / dt rounds either way near an integer)
+    cfg = CONFIGS[run] + f"tf = {(steps + 1) * dt!r}\nnsteps = {steps}\noutput_interval = 1000000\n"
     run_app(tmp_path, cfg, "kat")
     got = parse_log(open(tmp_path / "output" / "logs" / "kat.txt").read())
     assert len(got) == steps
@@ -119,7 +119,8 @@ def test_program_reproduces_shipped_redblack_logs(tmp_path, run):
 @pytest.mark.gpu
 def test_program_writes_reference_vtk_files(tmp_path, orc):
     n, steps, interval, dt = 32, 7, 3, 0.004
-    cfg = (f"Re = 400.0\nnx = {n}\nny = {n}\ndt = {dt!r}\ntf = {(steps + 1) * dt!r}\npoisson_tol = 1E-8\n"
+    cfg = (f"Re = 400.0\nnx = {n}\nny = {n}\ndt = {dt!r}\ntf = {(steps + 1) * dt!r}\nnsteps = {steps}\n"
+           f"poisson_tol = 1E-8\n"
            f"poisson_max_it = 100000\noutput_interval = {interval}\n")
     run_app(tmp_path, cfg, "vtk")
     files = sorted(os.listdir(tmp_path / "output" / "vtk"))
