@@ -46,6 +46,10 @@ int fail(int status, const char* fmt, ...) {
                         __FILE__, __LINE__);                                                  \
     } while (0)
 
+// Sweeps per border exchange the FP64 SOR/GS solve uses by default for an n x n grid (1: the
+// kernel that exchanges every half-sweep).
+int auto_sor_sweeps(int n) { return n <= 768 ? 4 : 1; }
+
 bool is_pow2(double x) {
     int e;
     return x > 0 && std::frexp(x, &e) == 0.5;
@@ -112,6 +116,13 @@ struct cnv_state {
     int mixed_gx = 1, mixed_gy = 1, mixed_epochs = 1, mixed_max_outer = 100;
     bool mixed_rq_smem = false;
     double mixed_rtol = 1e-10;
+    // several sweeps per border exchange (FP64 SOR/GS in shared-memory tiles)
+    bool tb = false;
+    int tb_sweeps = 4;
+    int tb_gx = 1, tb_gy = 1;
+    bool tb_g_smem = false;
+    double* tb_snap = nullptr;
+    void* tb_sync = nullptr;
     // exact solve by sine transforms (CNV_POISSON_DIRECT)
     bool direct = false;
     DstPlan dst{};
@@ -152,6 +163,8 @@ void free_state(cnv_state* s) {
     for (float* b : {s->rq, s->eg})
         if (b) cudaFree(b);
     if (s->msync) cudaFree(s->msync);
+    if (s->tb_snap) cudaFree(s->tb_snap);
+    if (s->tb_sync) cudaFree(s->tb_sync);
     if (s->direct) dst_plan_destroy(&s->dst);
     if (s->flag) cudaFree(s->flag);
     if (s->sync) cudaFree(s->sync);
@@ -173,6 +186,9 @@ int validate(const cnv_config* c) {
         return fail(CNV_BAD_ARG, "grid size %d outside [%d, 16384]", c->nx, c->order == 6 ? 5 : 4);
     if (c->poisson_type < 1 || c->poisson_type > 4)
         return fail(CNV_BAD_ARG, "Error - invalid option for Poisson solver (%d)", c->poisson_type);
+    if (c->sor_blocking != 0 && c->sor_blocking != 1 && c->sor_blocking != 2 && c->sor_blocking != 4)
+        return fail(CNV_BAD_ARG, "sor_blocking must be 0 (auto), 1, 2 or 4 sweeps per exchange, got %d",
+                    c->sor_blocking);
     if (c->poisson_type == CNV_POISSON_DIRECT && c->precision == CNV_PREC_MIXED)
         return fail(CNV_BAD_ARG, "the direct Poisson solve is FP64 only (precision %d)", c->precision);
     if (c->precision != CNV_PREC_FP64 && c->precision != CNV_PREC_FP64_FMA && c->precision != CNV_PREC_MIXED)
@@ -295,6 +311,25 @@ int enqueue_poisson(cnv_state* s, const double* in, double scale) {
         static_assert(offsetof(Ctrl, status) == offsetof(Ctrl, iters) + 4 && offsetof(Ctrl, err) == offsetof(Ctrl, iters) + 8,
                       "Ctrl layout");
         CNV_CUDA(cudaMemsetAsync(reinterpret_cast<char*>(s->ctrl) + offsetof(Ctrl, iters), 0, 16, s->stream));
+        return CNV_OK;
+    }
+    if (s->tb) {
+        CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
+        CNV_CUDA(cudaMemsetAsync(s->sor[1], 0, split_bytes, s->stream));
+        TbLaunch T{};
+        T.p = s->pp;
+        T.sweeps = s->tb_sweeps;
+        T.gx = s->tb_gx;
+        T.gy = s->tb_gy;
+        T.g_in_smem = s->tb_g_smem ? 1 : 0;
+        T.out[0] = s->sor[0];
+        T.out[1] = s->sor[1];
+        T.rhs[0] = s->rhs[0];
+        T.rhs[1] = s->rhs[1];
+        T.snap = s->tb_snap;
+        T.ctrl = s->ctrl;
+        T.sync = s->tb_sync;
+        CNV_CUDA(launch_poisson_tb(T, s->stream));
         return CNV_OK;
     }
     if (s->mixed) {
@@ -501,6 +536,36 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
         }
     }
 #undef ALLOC
+    // several sweeps per exchange: one block per SM, tiles at least as wide as the halo, the
+    // psi tile (and the right-hand side when it also fits) in shared memory
+    const int want_sweeps = cfg->sor_blocking == 0 ? auto_sor_sweeps(n) : cfg->sor_blocking;
+    if (!s->mixed && cfg->poisson_type != CNV_POISSON_DIRECT && cfg->poisson_type != CNV_POISSON_JACOBI &&
+        want_sweeps > 1) {
+        s->tb_sweeps = want_sweeps;
+        int g = cfg->solver_blocks > 0 ? std::min(cfg->solver_blocks, s->sms) : s->sms;
+        for (; g >= 1; --g) {
+            poisson_tiles(n, g, &s->tb_gx, &s->tb_gy);
+            if (tb_tiles_ok(n, s->tb_gx, s->tb_gy, want_sweeps)) break;
+        }
+        const size_t optin = prop.sharedMemPerBlockOptin;
+        const bool fits = g >= 1 && tb_smem_bytes(n, s->tb_gx, s->tb_gy, want_sweeps, false) + 2048 <= optin;
+        if (fits) {
+            s->tb = true;
+            s->tb_g_smem = tb_smem_bytes(n, s->tb_gx, s->tb_gy, want_sweeps, true) + 2048 <= optin;
+            const size_t snap = tb_snapshot_doubles(n, s->pitch);
+            if (cudaMalloc(&s->tb_snap, snap * sizeof(double)) != cudaSuccess ||
+                cudaMalloc(&s->tb_sync, tb_sync_bytes()) != cudaSuccess) {
+                free_state(s);
+                return fail(CNV_CUDA_ERROR, "cudaMalloc failed (tiled solver buffers)");
+            }
+        } else if (cfg->sor_blocking > 1) {
+            free_state(s);
+            return fail(CNV_BAD_ARG, "grid %d too large or too small for shared-memory SOR tiles", n);
+        }
+    } else if (cfg->sor_blocking > 1) {
+        free_state(s);
+        return fail(CNV_BAD_ARG, "sor_blocking > 1 needs the FP64 SOR or Gauss-Seidel solver");
+    }
     if (cfg->poisson_type == CNV_POISSON_DIRECT) {
         s->direct = true;
         if (dst_plan_create(n, s->dx, s->dy, &s->dst) != CNV_OK) {

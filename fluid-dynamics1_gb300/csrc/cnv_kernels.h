@@ -89,6 +89,28 @@ size_t mixed_smem_bytes(int n, int gx, int gy, bool rq_in_smem);
 int mixed_threads();
 int mixed_sweeps_per_exchange();
 
+// Persistent red-black SOR / GS with 2 or 4 sweeps per border exchange (cnv_poisson_tb.cu):
+// the same bits as launch_poisson, with each tile (plus a halo) in shared memory. out = the
+// answer (split layout, zeroed edges), snap = tb_snapshot_doubles() of scratch, sync =
+// tb_sync_bytes() (zeroed by the launch). One block of tb_threads() per tile, all co-resident.
+struct TbLaunch {
+    PoissonParams p;
+    int sweeps;     // sweeps per exchange: 2 or 4 (halo 2 * sweeps)
+    int gx, gy;
+    int g_in_smem;  // keep the right-hand side tile in shared memory too
+    double* out[2];
+    const double* rhs[2];
+    double* snap;
+    Ctrl* ctrl;
+    void* sync;
+};
+cudaError_t launch_poisson_tb(const TbLaunch& L, cudaStream_t s);
+int tb_threads();
+size_t tb_sync_bytes();
+size_t tb_snapshot_doubles(int n, int pitch);
+size_t tb_smem_bytes(int n, int gx, int gy, int sweeps, bool g_smem);
+bool tb_tiles_ok(int n, int gx, int gy, int sweeps);
+
 // Tile factorisation grid = gx * gy for an n x n grid (tiles near-square, at least 64 wide when
 // possible).
 void poisson_tiles(int n, int grid, int* gx, int* gy);

@@ -145,29 +145,34 @@ size_t mixed_smem_bytes(int n, int gx, int gy, bool rq_in_smem) {
 
 namespace {
 
+// The dynamic shared memory of k_mixed. The hot loop addresses it through this array with
+// integer offsets, so every access compiles to a shared-memory load or store.
+extern __shared__ float mx_smem[];
+
 // One colour c of an FP32 red-black SOR half-sweep on rows [lo_r, hi_r), columns [lo_c, hi_c) of
-// the shared-memory tile (split layout: row r of colour k at sc/so[(i - sr0) * swm + (m - m0)]).
-// The correction right-hand side comes from the shared-memory tile (RQ_SMEM) or from L2. Kept
-// out of line so that it gets its own register allocation: it is the hot loop of the solve.
+// the shared-memory tile (split layout: row i of colour k at mx_smem[k_off + (i - sr0) * swm + (m -
+// m0)]): e of colour c at sc_off, of the other colour at so_off; the correction right-hand side
+// R/den at rq_off in shared memory (RQ_SMEM) or in the global split array rq (pitch P). Kept out
+// of line so that it gets its own register allocation: it is the hot loop of the solve.
 template <bool RQ_SMEM>
-__device__ __noinline__ void mixed_half_sweep(float* __restrict__ sc, const float* __restrict__ so,
-                                              const float* __restrict__ rq, int sr0, int swm, int m0,
-                                              int lo_r, int hi_r, int lo_c, int hi_c, int c, int P,
-                                              float wx, float wy, float beta) {
+__device__ __noinline__ void mixed_half_sweep(int sc_off, int so_off, int rq_off, const float* __restrict__ rq,
+                                              int sr0, int swm, int m0, int lo_r, int hi_r, int lo_c, int hi_c,
+                                              int c, int P, float wx, float wy, float beta) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int i = lo_r + warp; i < hi_r; i += kWarps) {
         const int q = (i + c) & 1;
         const int mlo = floor_half(lo_c - q + 1), mhi = floor_half(hi_c - 1 - q);
         const int row = (i - sr0) * swm - m0;
-        const float* rqrow = RQ_SMEM ? rq + row : rq + (size_t)i * P;
+        const float* rqrow = rq + (size_t)i * P;
         for (int m = mlo + lane; m <= mhi; m += 32) {
-            const float up = so[row + swm + m], dn = so[row - swm + m];
-            const float lt = so[row + m - 1 + q], rt = so[row + m + q];
+            const int k = row + m;
+            const float up = mx_smem[so_off + k + swm], dn = mx_smem[so_off + k - swm];
+            const float lt = mx_smem[so_off + k - 1 + q], rt = mx_smem[so_off + k + q];
             // R/den: shared-memory copy, or L2 (rewritten every outer iteration)
-            const float r = RQ_SMEM ? rqrow[m] : __ldcg(rqrow + m);
-            const float me = sc[row + m];
+            const float r = RQ_SMEM ? mx_smem[rq_off + k] : __ldcg(rqrow + m);
+            const float me = mx_smem[sc_off + k];
             const float gs = fmaf(wy, up + dn, fmaf(wx, lt + rt, -r));
-            sc[row + m] = fmaf(beta, gs - me, me);
+            mx_smem[sc_off + k] = fmaf(beta, gs - me, me);
         }
     }
 }
@@ -175,7 +180,7 @@ __device__ __noinline__ void mixed_half_sweep(float* __restrict__ sc, const floa
 __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
     Ctrl* ctl = L.ctrl;
     if (ctl->abort) return;
-    extern __shared__ float s_mem[];
+    float* const s_mem = mx_smem;
     __shared__ int s_ok;
     __shared__ int s_flag[8];
     __shared__ double s_red[kWarps][2];
@@ -299,24 +304,22 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
                 __syncthreads();
                 for (int q = 0; q < 8; ++q) ok = ok && s_flag[q];
                 if (!ok) break;
+                // one flat loop over the tile-plus-halo box: every thread issues its few
+                // independent L2 loads at once (a warp walking rows would wait for each in turn)
                 const int par = (ep - 1) & 1;
-                for (int r = warp; r < S.sh; r += kWarps) {
+                const int box = S.sh * S.swm;
+                for (int x = threadIdx.x; x < box; x += kThreads) {
+                    const int r = x / S.swm;
                     const int i = S.sr0 + r;
                     if (i < 1 || i > n - 2) continue;
+                    const int m = S.m0 + (x - r * S.swm);
                     const bool own_row = i >= t.r0 && i < t.r1;
+#pragma unroll
                     for (int c = 0; c < 2; ++c) {
-                        const int q = (i + c) & 1;
-                        const float* src = L.eg[par][c] + (size_t)i * P;
-                        // halo columns of this row: all of [c0-H, c1+H) for rows outside the
-                        // tile, else the two side strips; clipped to the interior
-                        for (int seg = 0; seg < (own_row ? 2 : 1); ++seg) {
-                            int jlo = own_row ? (seg ? t.c1 : t.c0 - kHalo) : t.c0 - kHalo;
-                            int jhi = own_row ? (seg ? t.c1 + kHalo : t.c0) : t.c1 + kHalo;
-                            jlo = max(jlo, 1);
-                            jhi = min(jhi, n - 1);
-                            const int mlo = floor_half(jlo - q + 1), mhi = floor_half(jhi - 1 - q);
-                            for (int m = mlo + lane; m <= mhi; m += 32) S.at(c, i, m) = __ldcg(src + m);
-                        }
+                        const int j = 2 * m + ((i + c) & 1);
+                        if (j < max(1, t.c0 - kHalo) || j >= min(n - 1, t.c1 + kHalo)) continue;
+                        if (own_row && j >= t.c0 && j < t.c1) continue;  // own cell: already current
+                        S.at(c, i, m) = __ldcg(L.eg[par][c] + (size_t)i * P + m);
                     }
                 }
                 __syncthreads();
@@ -325,32 +328,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_mixed(MixedLaunch L) {
                 const int c = (s - 1) & 1;  // red first
                 const int lo_r = max(1, t.r0 - kHalo + s), hi_r = min(n - 1, t.r1 + kHalo - s);
                 const int lo_c = max(1, t.c0 - kHalo + s), hi_c = min(n - 1, t.c1 + kHalo - s);
+                const int plane = S.sh * S.swm;  // e colour k at k * plane, R/den colour k at (2 + k) * plane
                 if (srq)
-                    mixed_half_sweep<true>(S.c[c], S.c[c ^ 1], srq + c * (S.sh * S.swm), S.sr0, S.swm, S.m0,
-                                           lo_r, hi_r, lo_c, hi_c, c, P, wx, wy, beta);
+                    mixed_half_sweep<true>(c * plane, (c ^ 1) * plane, (2 + c) * plane, L.rq[c], S.sr0, S.swm,
+                                           S.m0, lo_r, hi_r, lo_c, hi_c, c, P, wx, wy, beta);
                 else
-                    mixed_half_sweep<false>(S.c[c], S.c[c ^ 1], L.rq[c], S.sr0, S.swm, S.m0, lo_r, hi_r,
-                                            lo_c, hi_c, c, P, wx, wy, beta);
+                    mixed_half_sweep<false>(c * plane, (c ^ 1) * plane, 0, L.rq[c], S.sr0, S.swm, S.m0, lo_r,
+                                            hi_r, lo_c, hi_c, c, P, wx, wy, beta);
                 __syncthreads();
             }
             sweeps += kSweepsPerExchange;
             if (e + 1 < L.epochs) {
                 // own border strips (width H) -> global copy of this epoch; raise the flag
                 const int par = ep & 1;
-                for (int i = t.r0 + warp; i < t.r1; i += kWarps) {
-                    const bool edge_row = i < t.r0 + kHalo || i >= t.r1 - kHalo;
-                    for (int c = 0; c < 2; ++c) {
-                        const int q = (i + c) & 1;
-                        float* dst = L.eg[par][c] + (size_t)i * P;
-                        // border columns: the whole row near the top/bottom edge, else the two
-                        // side strips of width H
-                        for (int seg = 0; seg < (edge_row ? 1 : 2); ++seg) {
-                            const int jlo = edge_row ? t.c0 : (seg ? max(t.c1 - kHalo, t.c0) : t.c0);
-                            const int jhi = edge_row ? t.c1 : (seg ? t.c1 : min(t.c0 + kHalo, t.c1));
-                            const int mlo = floor_half(jlo - q + 1), mhi = floor_half(jhi - 1 - q);
-                            for (int m = mlo + lane; m <= mhi; m += 32) dst[m] = S.at(c, i, m);
-                        }
-                    }
+                const int tw = t.c1 - t.c0, th = t.r1 - t.r0;
+                for (int x = threadIdx.x; x < tw * th; x += kThreads) {
+                    const int r = x / tw;
+                    const int i = t.r0 + r;
+                    const int j = t.c0 + (x - r * tw);
+                    if (i >= t.r0 + kHalo && i < t.r1 - kHalo && j >= t.c0 + kHalo && j < t.c1 - kHalo) continue;
+                    const int c = (i + j) & 1;
+                    L.eg[par][c][(size_t)i * P + (j >> 1)] = S.at(c, i, j >> 1);
                 }
                 __syncthreads();
                 if (threadIdx.x == 0) st_release(&sy->flag[blockIdx.x], ep);

@@ -37,6 +37,7 @@
 #include <cfloat>
 
 #include "cnv_kernels.h"
+#include "cnv_sor.cuh"
 
 namespace cnv {
 namespace {
@@ -58,174 +59,6 @@ struct SyncState {
     unsigned int nonfinite[kRing];
     unsigned int flag[2][kMaxSolverBlocks];  // [colour][block]: last sweep whose frame is written
 };
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-__device__ __forceinline__ long long globaltimer_ns() {
-    long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ int ld_volatile_int(const int* p) { return *(const volatile int*)p; }
-
-// Wait until *p >= want (as sweep counters). Returns false on timeout or abort.
-__device__ bool wait_geq(const unsigned* p, unsigned want, Ctrl* ctl, long long timeout_ns) {
-    long long t0 = 0;
-    int polls = 0;
-    while ((int)(ld_acquire(p) - want) < 0) {
-        if (ld_volatile_int(&ctl->abort)) return false;
-        if (++polls == 64) t0 = globaltimer_ns();
-        if (polls > 64 && globaltimer_ns() - t0 > timeout_ns) {
-            atomicExch(&ctl->status, CNV_TIMEOUT);
-            atomicExch(&ctl->abort, 1);
-            return false;
-        }
-    }
-    return true;
-}
-
-// exact 128-bit fixed-point image (scale 2^80, truncated) of a non-negative double
-__device__ __forceinline__ void to_fixed96(double x, unsigned long long& lo, unsigned long long& hi) {
-    lo = hi = 0;
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const int ex = (int)((b >> 52) & 0x7ff);
-    if (ex == 0 || ex == 0x7ff || (b >> 63)) return;  // zero, subnormal (< 2^-1022), inf/nan, negative
-    const unsigned long long mant = (b & ((1ull << 52) - 1)) | (1ull << 52);
-    const int s = ex - 1075 + 80;  // value * 2^80 = mant * 2^s
-    if (s >= 64 + 11) {            // would not fit 128 bits: saturate
-        lo = ~0ull;
-        hi = ~0ull >> 1;
-    } else if (s >= 64) {
-        hi = mant << (s - 64);
-    } else if (s > 0) {
-        lo = mant << s;
-        hi = mant >> (64 - s);
-    } else if (s > -53) {
-        lo = mant >> (-s);
-    }
-}
-
-__device__ __forceinline__ double from_fixed96(unsigned long long lo, unsigned long long hi) {
-    return (double)hi * 0x1.0p-16 + (double)lo * 0x1.0p-80;
-}
-
-// Stop-norm accumulator of one thread: |psi_new - psi_old| summed exactly as integers in units
-// of 2^-80, in four 32-bit chunks held by 64-bit counters (no carries while accumulating).
-struct NormAcc {
-    unsigned long long c[4];
-    unsigned int big;  // set if a value reached 2^46 (outside the fixed-point range)
-};
-
-// |x| * 2^80, truncated, as a 128-bit integer (hi:lo); values below 2^-80 give 0.
-__device__ __forceinline__ void abs_fixed80(double x, unsigned long long& lo, unsigned long long& hi,
-                                            unsigned int& big) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
-    const int ex = (int)(b >> 52);
-    const unsigned long long mant = (b & ((1ull << 52) - 1)) | (1ull << 52);
-    const int s = ex - 995;  // |x| * 2^80 = mant * 2^s
-    lo = 0;
-    hi = 0;
-    if (ex == 0) return;     // zero or below 2^-1022
-    if (s >= 74) {           // |x| >= 2^46 (also inf/nan)
-        big = 1;
-        return;
-    }
-    if (s >= 64) {
-        hi = mant << (s - 64);
-    } else if (s > 0) {
-        lo = mant << s;
-        hi = mant >> (64 - s);
-    } else if (s > -53) {
-        lo = mant >> (-s);
-    }
-}
-
-// acc += |nw - old|, exactly in fixed point (both truncated at 2^-80), on the integer pipes.
-__device__ __forceinline__ void norm_add(NormAcc& acc, double nw, double old) {
-    unsigned long long al, ah, bl, bh;
-    abs_fixed80(nw, al, ah, acc.big);
-    abs_fixed80(old, bl, bh, acc.big);
-    unsigned long long dl, dh;
-    if ((__double_as_longlong(nw) ^ __double_as_longlong(old)) < 0) {  // opposite signs: |a| + |b|
-        dl = al + bl;
-        dh = ah + bh + (dl < al);
-    } else {  // same sign: ||a| - |b||
-        const bool a_ge = ah > bh || (ah == bh && al >= bl);
-        if (a_ge) {
-            dl = al - bl;
-            dh = ah - bh - (al < bl);
-        } else {
-            dl = bl - al;
-            dh = bh - ah - (bl < al);
-        }
-    }
-    acc.c[0] += dl & 0xffffffffull;
-    acc.c[1] += dl >> 32;
-    acc.c[2] += dh & 0xffffffffull;
-    acc.c[3] += dh >> 32;
-}
-
-__device__ __forceinline__ bool big_or_zero(double x) {
-    // |x| >= 2^-960 (biased exponent >= 63) or x == +-0
-    const int hi = __double2hiint(x);
-    const int lo = __double2loint(x);
-    return ((hi & 0x7ff00000) >= (63 << 20)) || (((hi & 0x7fffffff) | lo) == 0);
-}
-
-template <Arith A, int KIND, bool FOLD>
-__device__ __forceinline__ double point_update(const PoissonParams& p, double up, double dn, double rt,
-                                               double lt, double g, double old, NormAcc& acc) {
-    double nw;
-    if (A == Arith::kExact) {
-        if (FOLD) {
-            // g holds c4*f/dx^2 (exact power-of-two scaling of the reference's c4*f)
-            const double s1 = __dadd_rn(up, dn);
-            const double s2 = __dadd_rn(rt, lt);
-            const double S = __dadd_rn(s1, s2);
-            const double t = __dsub_rn(S, g);
-            if (big_or_zero(s1) && big_or_zero(s2) && big_or_zero(S) && big_or_zero(t)) {
-                if (KIND == CNV_POISSON_SOR)
-                    nw = __dadd_rn(__dmul_rn(p.b4, t), __dmul_rn(p.omb, old));
-                else
-                    nw = __dmul_rn(0.25, t);
-            } else {
-                const double gr = __dmul_rn(g, p.dx2);  // back to c4*f exactly
-                const double num = __dsub_rn(__dadd_rn(__dmul_rn(p.dy2, s1), __dmul_rn(p.dx2, s2)), gr);
-                if (KIND == CNV_POISSON_SOR)
-                    nw = __dadd_rn(__dmul_rn(__dmul_rn(p.beta, num), p.rden), __dmul_rn(p.omb, old));
-                else
-                    nw = __dmul_rn(num, p.rden);
-            }
-        } else {
-            // beta*(dy*dy*(up+dn) + dx*dx*(rt+lt) - dx*dx*dy*dy*f) / (2*(dx*dx+dy*dy)) + (1-beta)*u0
-            const double num = __dsub_rn(__dadd_rn(__dmul_rn(p.dy2, __dadd_rn(up, dn)),
-                                                   __dmul_rn(p.dx2, __dadd_rn(rt, lt))), g);
-            if (KIND == CNV_POISSON_SOR) {
-                const double bn = __dmul_rn(p.beta, num);
-                const double q = p.den_pow2 ? __dmul_rn(bn, p.rden) : __ddiv_rn(bn, p.den);
-                nw = __dadd_rn(q, __dmul_rn(p.omb, old));
-            } else {
-                nw = p.den_pow2 ? __dmul_rn(num, p.rden) : __ddiv_rn(num, p.den);
-            }
-        }
-        norm_add(acc, nw, old);
-        return nw;
-    } else {
-        const double gs = fma(p.wy, up + dn, fma(p.wx, rt + lt, -g));
-        nw = KIND == CNV_POISSON_SOR ? fma(p.beta, gs - old, old) : gs;
-        norm_add(acc, nw, old);
-        return nw;
-    }
-}
 
 struct Tile {
     int r0, r1, c0, c1;  // tile rows [r0, r1), columns [c0, c1) (absolute indices)

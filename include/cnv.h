@@ -97,7 +97,10 @@ typedef struct cnv_config {
     int solver_blocks;       /* Poisson solver blocks (tiles); <= 0 picks them from the grid size */
     int mixed_inner_sweeps;  /* CNV_PREC_MIXED: FP32 sweeps per correction; <= 0 picks n */
     int mixed_max_outer;     /* CNV_PREC_MIXED: correction limit (CNV_NOT_CONVERGED past it); <= 0: 100 */
-    int reserved[5];
+    int sor_blocking;        /* FP64 SOR/GS kernel, by sweeps per border exchange: 0 auto, 1 exchange
+                                every half-sweep, 2 or 4 sweeps per exchange on shared-memory tiles
+                                (the same bits either way) */
+    int reserved[4];
 } cnv_config;
 
 /* Per-step record: the values the reference logs (src/poisson.c:275, src/main.c:407-408). */

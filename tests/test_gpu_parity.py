@@ -1,5 +1,9 @@
 """CUDA path vs the CPU oracle, through the C ABI of libcnv.
 
+Both FP64 SOR/GS kernels are checked where it matters (sor_blocking = 1: border exchange every
+half-sweep; 2 or 4: that many sweeps per exchange on shared-memory tiles, grids with
+n - 2 >= 2 * sweeps).
+
 Tolerances: the FP64 path with reference arithmetic (precision = fp64) must match the oracle
 bit for bit on every field (same operation order, round-to-nearest, no FMA contraction);
 iteration counts must be equal; the stop norm is summed in a different order on the GPU, so it
@@ -35,6 +39,13 @@ def oracle_params(orc, cfg, ordering=1):
                            tol=cfg.poisson_tol, threads=0, exact_norm=0)
 
 
+BLOCKING = [1, 2, 4]
+
+
+def blocking_ok(n, blocking):
+    return blocking == 1 or n - 2 >= 2 * blocking
+
+
 def bitwise(a, b):
     return np.array_equal(np.asarray(a).view(np.uint64), np.asarray(b).view(np.uint64))
 
@@ -50,9 +61,12 @@ def run_both(cnv, orc, cfg, nsteps):
     return (gw, gu, gv, gpsi), gsteps, (w, u, v, psi), osteps
 
 
+@pytest.mark.parametrize("blocking", BLOCKING)
 @pytest.mark.parametrize("n,order", [(7, 6), (8, 6), (16, 6), (33, 6), (64, 6), (32, 4), (32, 2), (5, 6), (4, 4)])
-def test_step_bitwise_equals_oracle(cnv, orc, n, order):
-    cfg = make_cfg(cnv, n, order=order)
+def test_step_bitwise_equals_oracle(cnv, orc, n, order, blocking):
+    if not blocking_ok(n, blocking):
+        pytest.skip("grid smaller than one shared-memory tile")
+    cfg = make_cfg(cnv, n, order=order, sor_blocking=blocking)
     g, gs, o, os_ = run_both(cnv, orc, cfg, 6)
     for name, a, b in zip("w u v psi".split(), g, o):
         assert bitwise(a, b), f"{name} differs: max abs {np.max(np.abs(a - b))}"
@@ -62,27 +76,32 @@ def test_step_bitwise_equals_oracle(cnv, orc, n, order):
         assert bitwise(a["cont_max"], b["cont_max"]) and bitwise(a["cont_min"], b["cont_min"])
 
 
-@pytest.mark.parametrize("n,blocks", [(64, 4), (64, 16), (64, 37), (64, 152), (50, 9), (130, 304), (31, 6)])
-def test_step_bitwise_with_forced_tilings(cnv, orc, n, blocks):
-    """Many solver tiles on small grids: every tile frame and neighbour wait is exercised."""
-    cfg = make_cfg(cnv, n, solver_blocks=blocks, poisson_tol=1e-6)
+@pytest.mark.parametrize("blocking", BLOCKING)
+@pytest.mark.parametrize("n,blocks", [(64, 4), (64, 16), (64, 37), (64, 152), (50, 9), (130, 304), (31, 6),
+                                      (100, 7), (200, 60)])
+def test_step_bitwise_with_forced_tilings(cnv, orc, n, blocks, blocking):
+    """Many solver tiles on small grids: every tile frame, halo and neighbour wait is exercised
+    (the shared-memory kernel lowers the block count until tiles are at least 8 cells wide)."""
+    cfg = make_cfg(cnv, n, solver_blocks=blocks, poisson_tol=1e-6, sor_blocking=blocking)
     g, gs, o, os_ = run_both(cnv, orc, cfg, 4)
     for name, a, b in zip("w u v psi".split(), g, o):
         assert bitwise(a, b), f"{name} differs: max abs {np.max(np.abs(a - b))}"
     assert [s["iters"] for s in gs] == [s["iters"] for s in os_]
 
 
-@pytest.mark.parametrize("ptype", [1, 3])
-def test_gs_and_jacobi_steps_with_tiles(cnv, orc, ptype):
-    cfg = make_cfg(cnv, 48, poisson_type=ptype, solver_blocks=12, poisson_tol=1e-5, poisson_max_it=100000)
+@pytest.mark.parametrize("ptype,blocking", [(1, 1), (1, 2), (1, 4), (3, 1)])
+def test_gs_and_jacobi_steps_with_tiles(cnv, orc, ptype, blocking):
+    cfg = make_cfg(cnv, 48, poisson_type=ptype, solver_blocks=12, poisson_tol=1e-5, poisson_max_it=100000,
+                   sor_blocking=blocking)
     g, gs, o, os_ = run_both(cnv, orc, cfg, 3)
     for name, a, b in zip("w u v psi".split(), g, o):
         assert bitwise(a, b), name
 
 
-def test_step_all_boundary_values_and_rectangular_spacing(cnv, orc):
+@pytest.mark.parametrize("blocking", BLOCKING)
+def test_step_all_boundary_values_and_rectangular_spacing(cnv, orc, blocking):
     cfg = make_cfg(cnv, 24, Lx=2, Ly=1, Re=400.0, dt=0.001, poisson_tol=1e-6, u1=0.1, u2=-0.2, u3=0.3,
-                   u4=1.0, v1=0.05, v2=-0.05, v3=0.02, v4=-0.03, ui=0.01, vi=-0.02)
+                   u4=1.0, v1=0.05, v2=-0.05, v3=0.02, v4=-0.03, ui=0.01, vi=-0.02, sor_blocking=blocking)
     g, gs, o, os_ = run_both(cnv, orc, cfg, 4)
     for a, b in zip(g, o):
         assert bitwise(a, b)
@@ -113,12 +132,12 @@ def test_config1_64_re100_sor15(cnv, orc):
     assert [s["iters"] for s in gs] == [s["iters"] for s in os_]
 
 
-@pytest.mark.parametrize("ptype", [1, 2, 3])
+@pytest.mark.parametrize("ptype,blocking", [(1, 1), (2, 1), (3, 1), (1, 2), (2, 2), (1, 4), (2, 4)])
 @pytest.mark.parametrize("n", [16, 37, 96])
-def test_poisson_alone_matches_oracle(cnv, orc, ptype, n):
+def test_poisson_alone_matches_oracle(cnv, orc, ptype, n, blocking):
     rng = np.random.default_rng(n * 10 + ptype)
     f = rng.standard_normal((n, n))
-    cfg = make_cfg(cnv, n, poisson_type=ptype, poisson_tol=1e-9, poisson_max_it=200000)
+    cfg = make_cfg(cnv, n, poisson_type=ptype, poisson_tol=1e-9, poisson_max_it=200000, sor_blocking=blocking)
     with cnv.Cavity(cfg) as cav:
         rc, psi, it, err = cav.poisson(f)
     p = oracle_params(orc, cfg)
@@ -129,9 +148,10 @@ def test_poisson_alone_matches_oracle(cnv, orc, ptype, n):
     assert abs(err - oerr) <= REL_ERR_TOL * oerr
 
 
+@pytest.mark.parametrize("blocking", BLOCKING)
 @pytest.mark.parametrize("n", [64, 100, 128])
-def test_fma_form_within_tolerance(cnv, orc, n):
-    cfg = make_cfg(cnv, n, precision=1, poisson_tol=1e-8)
+def test_fma_form_within_tolerance(cnv, orc, n, blocking):
+    cfg = make_cfg(cnv, n, precision=1, poisson_tol=1e-8, sor_blocking=blocking)
     g, gs, o, os_ = run_both(cnv, orc, cfg, 5)
     for name, a, b in zip("w u v psi".split(), g, o):
         scale = max(np.max(np.abs(b)), 1e-300)
@@ -140,12 +160,13 @@ def test_fma_form_within_tolerance(cnv, orc, n):
         assert abs(a["iters"] - b["iters"]) <= 1
 
 
-def test_1024_single_step_matches_oracle(cnv, orc):
+@pytest.mark.parametrize("blocking", BLOCKING)
+def test_1024_single_step_matches_oracle(cnv, orc, blocking):
     """The benchmark workload's grid (1024^2, Re 1000, dt by the stability rule, tol 1e-6), step 0."""
     n = 1024
     h = 1.0 / n
     dt = 0.2 * min(h * h * 1000.0 / 4, h / 1.0)
-    cfg = make_cfg(cnv, n, Re=1000.0, dt=dt, poisson_tol=1e-6, poisson_max_it=100000)
+    cfg = make_cfg(cnv, n, Re=1000.0, dt=dt, poisson_tol=1e-6, poisson_max_it=100000, sor_blocking=blocking)
     g, gs, o, os_ = run_both(cnv, orc, cfg, 1)
     for name, a, b in zip("w u v psi".split(), g, o):
         assert bitwise(a, b), name
@@ -153,12 +174,38 @@ def test_1024_single_step_matches_oracle(cnv, orc):
 
 
 # ------------------------------------------------------------------------- failure paths
-def test_itmax_reports_not_converged_and_stops(cnv):
-    cfg = make_cfg(cnv, 32, poisson_max_it=2, poisson_tol=1e-12)
+@pytest.mark.parametrize("blocking", BLOCKING)
+@pytest.mark.parametrize("itmax", [2, 9])
+def test_itmax_reports_not_converged_and_stops(cnv, blocking, itmax):
+    cfg = make_cfg(cnv, 32, poisson_max_it=itmax, poisson_tol=1e-12, sor_blocking=blocking)
     with cnv.Cavity(cfg) as cav:
         rc, steps = cav.step(3, raise_on_error=False)
     assert rc == cnv.CNV_NOT_CONVERGED
-    assert steps[0]["status"] == cnv.CNV_NOT_CONVERGED and steps[0]["iters"] == 2
+    assert steps[0]["status"] == cnv.CNV_NOT_CONVERGED and steps[0]["iters"] == itmax
+
+
+@pytest.mark.parametrize("blocking", BLOCKING)
+@pytest.mark.parametrize("tol", [1e3, 1e-1, 2e-3])
+def test_early_convergence_matches_oracle(cnv, orc, blocking, tol):
+    """Loose tolerances stop in the first sweeps (the shared-memory kernel then replays its first
+    epoch from zero) and at every position inside an epoch."""
+    rng = np.random.default_rng(7)
+    n = 40
+    f = rng.standard_normal((n, n))
+    cfg = make_cfg(cnv, n, poisson_tol=tol, sor_blocking=blocking)
+    with cnv.Cavity(cfg) as cav:
+        rc, psi, it, err = cav.poisson(f)
+    opsi, oit, oerr, orc_rc = orc.poisson(oracle_params(orc, cfg), f)
+    assert rc == 0 and orc_rc == 0 and it == oit
+    assert bitwise(psi, opsi)
+
+
+def test_blocking_flag_checks(cnv):
+    # argument checks need no GPU work: an unknown value, or blocking with a solver it cannot run
+    for kw in (dict(sor_blocking=3), dict(sor_blocking=4, poisson_type=3), dict(sor_blocking=4, nx=8, ny=8)):
+        with pytest.raises(cnv.CnvError) as e:
+            cnv.Cavity(make_cfg(cnv, kw.pop("nx", 32), **kw))
+        assert e.value.status == cnv.CNV_BAD_ARG
 
 
 def test_nonfinite_input_rejected(cnv):
