@@ -222,6 +222,7 @@ int upload_initial(cnv_state* s) {
     CNV_CUDA(cudaMemcpyAsync(s->v, v.data(), nn * 8, cudaMemcpyHostToDevice, s->stream));
     CNV_CUDA(cudaMemsetAsync(s->psi, 0, nn * 8, s->stream));
     CNV_CUDA(cudaMemsetAsync(s->w[1], 0, nn * 8, s->stream));
+    for (double* a : s->sor) CNV_CUDA(cudaMemsetAsync(a, 0, (size_t)n * s->pitch * 8, s->stream));
     CNV_CUDA(cudaStreamSynchronize(s->stream));
     return CNV_OK;
 }
@@ -301,7 +302,7 @@ MixedLaunch mixed_launch(cnv_state* s) {
 // Enqueue the Poisson solve on the split-layout rhs, or on g for the mixed form (psi starts
 // from zero). The direct solve reads the row-major field `in` scaled by `scale` instead
 // (w with c4 in a step, f with -c4 for a standalone solve) and reports 0 iterations.
-int enqueue_poisson(cnv_state* s, const double* in, double scale) {
+int enqueue_poisson(cnv_state* s, const double* in, double scale, bool in_step) {
     const size_t split_bytes = (size_t)s->n * s->pitch * 8;
     if (s->direct) {
         CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
@@ -333,8 +334,11 @@ int enqueue_poisson(cnv_state* s, const double* in, double scale) {
         return CNV_OK;
     }
     if (s->mixed) {
-        CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
-        CNV_CUDA(cudaMemsetAsync(s->sor[1], 0, split_bytes, s->stream));
+        // zero start, or (mixed_warm_start, within a time step) the previous step's psi
+        if (!(in_step && s->cfg.mixed_warm_start)) {
+            CNV_CUDA(cudaMemsetAsync(s->sor[0], 0, split_bytes, s->stream));
+            CNV_CUDA(cudaMemsetAsync(s->sor[1], 0, split_bytes, s->stream));
+        }
         CNV_CUDA(launch_mixed(mixed_launch(s), s->stream));
         return CNV_OK;
     }
@@ -397,7 +401,7 @@ int build_graphs(cnv_state* s) {
 int enqueue_step(cnv_state* s, int parity) {
     CNV_CUDA(cudaGraphLaunch(s->graph[0][parity], s->stream));
     CNV_CUDA(cudaEventRecord(s->evp0, s->stream));
-    int rc = enqueue_poisson(s, s->w[1 - parity], s->sa.c4);
+    int rc = enqueue_poisson(s, s->w[1 - parity], s->sa.c4, true);
     if (rc != CNV_OK) return rc;
     CNV_CUDA(cudaEventRecord(s->evp1, s->stream));
     CNV_CUDA(cudaGraphLaunch(s->graph[1][parity], s->stream));
@@ -820,7 +824,7 @@ int cnv_poisson_device(cnv_state* s, const double* f, double* psi_out, int* iter
     if (rc != CNV_OK) return rc;
     CNV_CUDA(launch_to_split(f, s->rhs[0], s->rhs[1], s->sa, s->stream));
     CNV_CUDA(cudaEventRecord(s->ev0, s->stream));
-    rc = enqueue_poisson(s, f, -s->sa.c4);
+    rc = enqueue_poisson(s, f, -s->sa.c4, false);
     if (rc != CNV_OK) return rc;
     CNV_CUDA(cudaEventRecord(s->ev1, s->stream));
     CNV_CUDA(launch_from_split(s->sor[0], s->sor[1], psi_out, s->n, s->pitch, s->stream));

@@ -60,6 +60,7 @@ struct BatchLaunch {
     int count;
     int max_outer;
     double rtol;
+    int warm;           // start each step's solve from the previous psi (mixed_warm_start)
     int smem_floats;    // dynamic shared memory available to a block (floats)
 };
 
@@ -126,7 +127,7 @@ __device__ void batch_half_sweep(float* __restrict__ ec, const float* __restrict
 }
 
 // One time step of one cavity by the whole block. Returns the step's status.
-__device__ int batch_step(CavityDesc& C, float* smem, int max_outer, double rtol, double* s_red) {
+__device__ int batch_step(CavityDesc& C, float* smem, int max_outer, double rtol, bool warm, double* s_red) {
     const int n = C.n, P = C.pitch;
     const int tid = threadIdx.x, nt = blockDim.x;
     double* w_in = C.w[C.cur];
@@ -158,8 +159,9 @@ __device__ int batch_step(CavityDesc& C, float* smem, int max_outer, double rtol
         if (i > 0 && i < n - 1 && j > 0 && j < n - 1)
             C.g[(i + j) & 1][(size_t)i * P + (j >> 1)] = dmul(C.c4, -wn);
     }
-    // psi = 0 (zero start; zero Dirichlet edge)
-    for (int k = tid; k < 2 * n * P; k += nt) (k < n * P ? C.psi[0] : C.psi[1])[k < n * P ? k : k - n * P] = 0.0;
+    // psi = 0 (zero start; zero Dirichlet edge), or the previous step's psi (warm start)
+    if (!warm)
+        for (int k = tid; k < 2 * n * P; k += nt) (k < n * P ? C.psi[0] : C.psi[1])[k < n * P ? k : k - n * P] = 0.0;
     __syncthreads();
 
     // mixed-precision Poisson solve (cnv_mixed.cu's scheme, whole cavity in one block)
@@ -267,7 +269,7 @@ __global__ void __launch_bounds__(kMaxBatchThreads) k_batch(BatchLaunch L) {
         }
         __syncthreads();
         for (int t = 0; t < nsteps; ++t) {
-            const int st = batch_step(C, smem, L.max_outer, L.rtol, s_red);
+            const int st = batch_step(C, smem, L.max_outer, L.rtol, L.warm != 0, s_red);
             if (threadIdx.x == 0) C.steps_done = t + 1;
             if (st != CNV_OK) break;
         }
@@ -299,6 +301,7 @@ struct cnv_batch {
     int smem_bytes = 0;
     int max_outer = 100;
     double rtol = 1e-10;
+    int warm = 0;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0;
@@ -341,6 +344,7 @@ int build_graph(cnv_batch* b) {
     L.count = b->count;
     L.max_outer = b->max_outer;
     L.rtol = b->rtol;
+    L.warm = b->warm;
     L.smem_floats = b->smem_bytes / 4;
     BCUDA(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem_bytes));
     cudaGraph_t g = nullptr;
@@ -442,6 +446,7 @@ int cnv_batch_create(const cnv_config* base, int count, const cnv_cavity_spec* s
     b->specs.assign(specs, specs + count);
     b->max_outer = base->mixed_max_outer > 0 ? base->mixed_max_outer : 100;
     b->rtol = base->mixed_rtol > 0 ? base->mixed_rtol : 1e-10;
+    b->warm = base->mixed_warm_start ? 1 : 0;
     auto cleanup = [&](int rc, const std::string& m) {
         cnv_batch_destroy(b);
         return bfail(rc, m);

@@ -100,7 +100,9 @@ typedef struct cnv_config {
     int sor_blocking;        /* FP64 SOR/GS kernel, by sweeps per border exchange: 0 auto, 1 exchange
                                 every half-sweep, 2 or 4 sweeps per exchange on shared-memory tiles
                                 (the same bits either way) */
-    int reserved[4];
+    int mixed_warm_start;    /* CNV_PREC_MIXED (and batches): start each step's solve from the previous
+                                step's psi instead of zero (same stop rule: FP64 relative residual) */
+    int reserved[3];
 } cnv_config;
 
 /* Per-step record: the values the reference logs (src/poisson.c:275, src/main.c:407-408). */

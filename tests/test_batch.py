@@ -85,3 +85,24 @@ def test_batch_tuned_shape_gives_the_same_fields(cnv):
     for a4, b4 in zip(ref, tuned):
         for a, b in zip(a4, b4):
             assert np.max(np.abs(a - b)) <= SAME_SCHEME_TOL * max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.gpu
+def test_warm_batch_equals_warm_single_cavity_runs(cnv):
+    base = cnv.default_config(mixed_rtol=1e-10, mixed_warm_start=1)
+    nsteps = 4
+    specs = SPECS[:3]
+    with cnv.Batch(base, specs) as bt:
+        rc, last = bt.step(nsteps)
+        fields = [bt.get_fields(k) for k in range(len(specs))]
+    assert rc == 0
+    for k, sp in enumerate(specs):
+        cfg = cnv.default_config(nx=sp["n"], ny=sp["n"], Re=sp["Re"], u4=sp["lid"],
+                                 dt=_stable_dt(sp["n"], sp["Re"], sp["lid"]), precision=cnv.PREC_MIXED,
+                                 mixed_rtol=1e-10, mixed_warm_start=1)
+        with cnv.Cavity(cfg) as cav:
+            _, steps = cav.step(nsteps)
+            single = cav.get_fields()
+        assert last[k]["iters"] == steps[-1]["iters"]
+        for name, a, b in zip("w u v psi".split(), fields[k], single):
+            assert np.max(np.abs(a - b)) <= SAME_SCHEME_TOL * np.max(np.abs(b)), (k, name)

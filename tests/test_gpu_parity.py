@@ -286,9 +286,11 @@ def test_mixed_poisson_reaches_fp64_residual(cnv, orc, n):
 
 
 @pytest.mark.parametrize("n", [64, 128])
-def test_mixed_steps_match_fp64_fields(cnv, orc, n):
-    """Time steps with the mixed solve against the FP64 oracle run to a tight tolerance."""
-    cfg = make_cfg(cnv, n, precision=cnv.PREC_MIXED, mixed_rtol=MIXED_RTOL, dt=0.001)
+@pytest.mark.parametrize("warm", [0, 1])
+def test_mixed_steps_match_fp64_fields(cnv, orc, n, warm):
+    """Time steps with the mixed solve (zero start or warm start from the previous step's psi)
+    against the FP64 oracle run to a tight tolerance."""
+    cfg = make_cfg(cnv, n, precision=cnv.PREC_MIXED, mixed_rtol=MIXED_RTOL, dt=0.001, mixed_warm_start=warm)
     with cnv.Cavity(cfg) as cav:
         rc, steps = cav.step(5)
         g = cav.get_fields()
@@ -300,3 +302,18 @@ def test_mixed_steps_match_fp64_fields(cnv, orc, n):
     orc.run(p, 5, w, u, v, psi)
     for name, a, b in zip("w u v psi".split(), g, (w, u, v, psi)):
         assert np.max(np.abs(a - b)) <= MIXED_FIELD_TOL * np.max(np.abs(b)), name
+
+
+def test_mixed_warm_start_needs_fewer_corrections(cnv):
+    # a slowly changing flow (tiny dt on a smooth noise field): the previous step's psi is
+    # already close, so the warm start needs fewer FP64 corrections to the same residual
+    n = 128
+    counts = {}
+    for warm in (0, 1):
+        cfg = make_cfg(cnv, n, precision=cnv.PREC_MIXED, mixed_rtol=MIXED_RTOL, dt=1e-7, mixed_warm_start=warm,
+                       init_field=cnv.INIT_NOISE, init_sigma=1.0, init_smooth_passes=8, seed=3)
+        with cnv.Cavity(cfg) as cav:
+            rc, steps = cav.step(6)
+        assert rc == 0
+        counts[warm] = sum(s["iters"] for s in steps[1:])
+    assert counts[1] < counts[0], counts
