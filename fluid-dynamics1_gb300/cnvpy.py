@@ -88,6 +88,8 @@ _SIGS = {
     "cnv_batch_reset": (C.c_int, [C.c_void_p]),
     "cnv_batch_tune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cnv_batch_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepInfo)]),
+    "cnv_batch_split": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "cnv_batch_groups": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "cnv_batch_get_fields": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
     "cnv_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),
     "cnv_adjoint_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(C.c_void_p)]),
@@ -294,6 +296,14 @@ class Batch:
         t, b = C.c_int(0), C.c_int(0)
         check(self._lib.cnv_batch_tune(self._h, C.byref(t), C.byref(b)), "cnv_batch_tune")
         return t.value, b.value
+
+    def split(self, factor: int, min_n: int = 1):
+        check(self._lib.cnv_batch_split(self._h, factor, min_n), "cnv_batch_split")
+
+    def groups(self):
+        out = (C.c_int * len(self.specs))()
+        check(self._lib.cnv_batch_groups(self._h, out), "cnv_batch_groups")
+        return list(out)
 
     def step(self, nsteps: int = 1, raise_on_error: bool = True):
         info = (StepInfo * len(self.specs))()

@@ -1,20 +1,29 @@
 // cnv_batch.cu -- many independent cavities (uneven grid size, Re and lid speed) advanced by one
 // persistent launch.
 //
-// Work unit: one cavity for `nsteps` time steps. Cavities are independent, so a block takes a
-// cavity from a queue (largest estimated cost first), integrates it for all the steps of the
-// call with no synchronisation beyond its own __syncthreads(), and takes the next. Each step is
-// the reference's loop body (src/main.c:283-395) with the same device arithmetic as the
-// single-cavity path (reference rounding for the wall, transport, velocity and continuity
-// passes) and the mixed-precision Poisson solve of cnv_mixed.cu: FP32 red-black SOR sweeps inside
-// FP64 defect correction to a relative FP64 residual. The FP32 correction lives in shared memory
-// when the cavity fits (together with its right-hand side when both fit), in the cavity's
-// global arrays otherwise.
+// Work unit: one cavity for `nsteps` time steps, run by a group of g blocks (g = 1 for most
+// cavities). Each step is the reference's loop body (src/main.c:283-395) with the same device
+// arithmetic as the single-cavity path (reference rounding for the wall, transport, velocity and
+// continuity passes) and the mixed-precision Poisson solve of cnv_mixed.cu: FP32 red-black SOR
+// sweeps inside FP64 defect correction to a relative FP64 residual.
 //
-// Launch shape (threads per block, blocks per SM) is picked by an autotuner that times one step
-// of each candidate from the initial state (cnv_batch_tune). The launch, with its queue reset, is
-// captured in a CUDA graph; the step count is read from device memory so one graph serves every
-// call.
+// One block (g = 1) keeps the FP32 correction in shared memory when the cavity fits (with its
+// right-hand side when both fit), in the cavity's global arrays otherwise. A cavity whose
+// correction does not fit one block's shared memory is split into g row strips, one per block of
+// its group: every pass runs on the block's strip, the FP32 correction of the strip plus a halo
+// of 2S rows lives in that block's shared memory, and the blocks meet at group barriers (global
+// counters with bounded waits): after the wall pass, after the transport pass, around each
+// residual norm, once per S FP32 sweeps to exchange border rows (the halo rows are recomputed, as
+// in cnv_mixed.cu, so the iterates equal global red-black sweeps), after the correction update,
+// after the velocity pass and after the continuity pass.
+//
+// Schedule. The host orders the jobs (largest estimated cost first) and places each on the g
+// blocks that become free first (longest-processing-time scheduling); every block runs its list
+// in start-time order, so members of a group reach their common job in the same global order and
+// no wait can close a cycle. The launch is cooperative (all blocks resident), captured in a CUDA
+// graph with the per-launch counters reset, and reads the step count from device memory so one
+// graph serves every call. The autotuner (cnv_batch_tune) times one step of each candidate
+// decomposition (strips only where shared memory needs them, or more) and keeps the fastest.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
@@ -44,18 +53,35 @@ struct CavityDesc {
     double* psi_rm;     // row-major psi (output)
     double* psi[2];     // split layout, FP64 iterate
     double* g[2];       // split layout, c4*f
-    float* e[2];        // split layout, FP32 correction (global mode)
-    float* rq[2];       // split layout, FP32 R/den (global mode)
+    float* e[2];        // split layout, FP32 correction (global mode); group jobs: border copies, parity 0
+    float* ex1[2];      // split layout, FP32 border copies of parity 1 (group jobs)
+    float* rq[2];       // split layout, FP32 R/den (global mode and group jobs)
     StepRecord last;    // record of the cavity's last step
     long long sweeps;   // FP32 sweeps done in the last call
     int steps_done;     // steps completed in the last call
-    int pad;
+    int group;          // blocks that run this cavity (row strips)
+};
+
+// Group barrier and reductions of one cavity's group (zeroed before every launch).
+constexpr int kMaxGroup = 16;
+struct GroupSync {
+    unsigned int bar;
+    unsigned int pad;
+    double part[kMaxGroup][2];  // per rank: residual and right-hand-side sums of squares
+    double cont[kMaxGroup][2];  // per rank: continuity max and min
+};
+
+// One entry of a block's job list: cavity, this block's strip (rank) and the group size.
+struct SchedEntry {
+    int cav, rank, group, pad;
 };
 
 struct BatchLaunch {
     CavityDesc* cav;
-    const int* order;   // processing order (largest cost first)
-    int* queue;         // next index into order (zeroed before each launch)
+    const SchedEntry* sched;  // job lists of all blocks, one after another
+    const int* sched_off;     // block b's list: sched[sched_off[b] .. sched_off[b+1])
+    GroupSync* gsync;         // one per cavity
+    int* abort;               // set when a group wait gives up (CNV_TIMEOUT)
     const int* nsteps;  // steps per cavity for this call (device memory)
     int count;
     int max_outer;
@@ -251,27 +277,326 @@ __device__ int batch_step(CavityDesc& C, float* smem, int max_outer, double rtol
     return status;
 }
 
+// ------------------------------------------------------------------------------ group jobs
+constexpr int kStripSweeps = 4;                // FP32 sweeps between border exchanges (as cnv_mixed.cu)
+constexpr int kStripHalo = 2 * kStripSweeps;   // halo rows of a strip
+
+__device__ __forceinline__ unsigned bt_ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ long long bt_now() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Barrier of the g blocks of a group (counter gs->bar, target gen). False if the wait gave up
+// (2 s; sets *abort = CNV_TIMEOUT) or another block has aborted; the caller leaves the job.
+__device__ bool group_barrier(GroupSync* gs, unsigned& gen, int g, int* abort, int* s_ok) {
+    __syncthreads();
+    gen += g;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&gs->bar, 1u);
+        int ok = 1, polls = 0;
+        long long t0 = 0;
+        while ((int)(bt_ld_acquire(&gs->bar) - gen) < 0) {
+            if (*(volatile int*)abort) {
+                ok = 0;
+                break;
+            }
+            if (++polls == 64) t0 = bt_now();
+            if (polls > 64 && bt_now() - t0 > 2000000000LL) {
+                atomicExch(abort, CNV_TIMEOUT);
+                ok = 0;
+                break;
+            }
+        }
+        __threadfence();
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+// FP32 red-black SOR half-sweep of colour c on rows [lo_r, hi_r) of a strip tile (rows from sr0,
+// split pitch ep, full interior width); R/den from the cavity's global array (pitch P, read
+// through L2: other blocks of the group write it). Same arithmetic as batch_half_sweep.
+__device__ void strip_half_sweep(float* __restrict__ ec, const float* __restrict__ eo, const float* __restrict__ rq,
+                                 int sr0, int ep, int P, int lo_r, int hi_r, int n, int c, float wx, float wy,
+                                 float beta) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int i = lo_r + warp; i < hi_r; i += nw) {
+        const int q = (i + c) & 1;
+        const int mlo = floor_half(1 - q + 1), mhi = floor_half(n - 2 - q);
+        const int row = (i - sr0) * ep;
+        const float* rrow = rq + (size_t)i * P;
+        for (int m = mlo + lane; m <= mhi; m += 32) {
+            const float up = eo[row + ep + m], dn = eo[row - ep + m];
+            const float lt = eo[row + m - 1 + q], rt = eo[row + m + q];
+            const float me = ec[row + m];
+            const float gs = fmaf(wy, up + dn, fmaf(wx, lt + rt, -__ldcg(rrow + m)));
+            ec[row + m] = fmaf(beta, gs - me, me);
+        }
+    }
+}
+
+// One time step of a cavity by block `r` of its group of g (rows [n r / g, n (r+1) / g)). Every
+// read of a field that other blocks of the group write goes through L2 (__ldcg). Returns the
+// step's status (the same in every block of the group); CNV_TIMEOUT if a group wait gave up.
+__device__ int group_step(CavityDesc& C, int cur, int r, int g, float* smem, int max_outer, double rtol, bool warm,
+                          double* s_red, GroupSync* gs, unsigned& gen, int* abort, int* s_ok, long long& sweeps,
+                          StepRecord& rec) {
+    const int n = C.n, P = C.pitch, sp = C.spitch;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int R0 = (int)((long long)n * r / g), R1 = (int)((long long)n * (r + 1) / g);
+    const int rows = R1 - R0;
+    double* const w_in = C.w[cur];
+    double* const w_out = C.w[cur ^ 1];
+    const BoundaryValues bc = C.bc;
+    const FdBands* B = C.bands;
+    auto LD = [](const double* p) { return __ldcg(p); };
+    auto U = [&](int y, int x) {
+        if (x == 0) return bc.u1;
+        if (x == n - 1) return bc.u2;
+        if (y == 0) return bc.u3;
+        if (y == n - 1) return bc.u4;
+        return LD(C.u + (size_t)y * n + x);
+    };
+    auto V = [&](int y, int x) {
+        if (x == 0) return bc.v1;
+        if (x == n - 1) return bc.v2;
+        if (y == 0) return bc.v3;
+        if (y == n - 1) return bc.v4;
+        return LD(C.v + (size_t)y * n + x);
+    };
+
+    // wall vorticity on the strip's edge cells (src/main.c:298-320), in place on w_in
+    {
+        const int top = R0 == 0 ? n - 2 : 0, bot = R1 == n ? n - 2 : 0;
+        const int total = 2 * rows + top + bot;
+        for (int x = tid; x < total; x += nt) {
+            int i, j;
+            if (x < 2 * rows) {
+                i = R0 + (x >> 1);
+                j = (x & 1) ? n - 1 : 0;
+            } else if (x < 2 * rows + top) {
+                i = 0;
+                j = 1 + (x - 2 * rows);
+            } else {
+                i = n - 1;
+                j = 1 + (x - 2 * rows - top);
+            }
+            w_in[(size_t)i * n + j] = dsub(along_j(B->d1x, n, i, j, V), along_i(B->d1y, n, i, j, U));
+        }
+    }
+    if (!group_barrier(gs, gen, g, abort, s_ok)) return CNV_TIMEOUT;
+    // transport on the strip's rows; g = c4 * (-w); psi = 0 on the strip's rows (zero start)
+    {
+        auto W = [&](int y, int x) { return LD(w_in + (size_t)y * n + x); };
+        for (int x = tid; x < rows * n; x += nt) {
+            const int i = R0 + x / n, j = x - (x / n) * n;
+            const double wx = along_j(B->d1x, n, i, j, W), wy = along_i(B->d1y, n, i, j, W);
+            const double wxx = along_j(B->d2x, n, i, j, W), wyy = along_i(B->d2y, n, i, j, W);
+            const double conv = dsub(dmul(-U(i, j), wx), dmul(V(i, j), wy));
+            const size_t k = (size_t)i * n + j;
+            const double wn = dadd(dmul(dadd(conv, dmul(C.inv_re, dadd(wxx, wyy))), C.dt), W(i, j));
+            w_out[k] = wn;
+            if (i > 0 && i < n - 1 && j > 0 && j < n - 1) C.g[(i + j) & 1][(size_t)i * P + (j >> 1)] = dmul(C.c4, -wn);
+        }
+        if (!warm)
+            for (int x = tid; x < 2 * rows * P; x += nt) {
+                const int c = x >= rows * P;
+                const int y = x - c * rows * P;
+                C.psi[c][(size_t)R0 * P + y] = 0.0;
+            }
+    }
+    if (!group_barrier(gs, gen, g, abort, s_ok)) return CNV_TIMEOUT;
+
+    // mixed-precision Poisson solve, the strip's FP32 correction (plus halo rows) in shared memory
+    const int ri0 = R0 > 1 ? R0 : 1, ri1 = R1 < n - 1 ? R1 : n - 1;  // own interior rows
+    const int sr0 = R0 - kStripHalo > 0 ? R0 - kStripHalo : 0;
+    const int sr1 = R1 + kStripHalo < n ? R1 + kStripHalo : n;
+    const int plane = (sr1 - sr0) * sp;
+    float* const es[2] = {smem, smem + plane};
+    const float wxf = (float)(C.dx2 / C.den), wyf = (float)(C.dy2 / C.den), betaf = (float)C.beta;
+    double rel = 0.0, gnorm = 0.0;
+    int outer = 0, status = CNV_NOT_CONVERGED;
+    const int epochs = C.inner / kStripSweeps;
+    for (outer = 0;; ++outer) {
+        double rr = 0.0, gg = 0.0;
+        for (int x = tid; x < (ri1 - ri0) * (n - 2); x += nt) {
+            const int i = ri0 + x / (n - 2), j = 1 + (x - (x / (n - 2)) * (n - 2));
+            const int c = (i + j) & 1, q = (i + c) & 1, m = j >> 1;
+            const double* pc = C.psi[c];
+            const double* po = C.psi[c ^ 1];
+            const size_t kk = (size_t)i * P + m;
+            const double gv = C.g[c][kk];
+            const double R = poisson_defect(C.dy2, C.dx2, C.den, LD(po + kk + P), LD(po + kk - P), LD(po + kk - 1 + q),
+                                            LD(po + kk + q), pc[kk], gv);
+            rr = fma(R, R, rr);
+            if (outer == 0) gg = fma(gv, gv, gg);
+            C.rq[c][kk] = (float)(R * C.rden);
+        }
+        rr = block_sum(rr, s_red);
+        if (outer == 0) gg = block_sum(gg, s_red);
+        if (tid == 0) {
+            gs->part[r][0] = rr;
+            if (outer == 0) gs->part[r][1] = gg;
+        }
+        if (!group_barrier(gs, gen, g, abort, s_ok)) return CNV_TIMEOUT;
+        {
+            double a = 0.0, b2 = 0.0;
+            for (int k = 0; k < g; ++k) {  // rank order: the same sum in every block
+                a += __ldcg(&gs->part[k][0]);
+                if (outer == 0) b2 += __ldcg(&gs->part[k][1]);
+            }
+            if (outer == 0) gnorm = sqrt(b2);
+            rel = gnorm > 0 ? sqrt(a) / gnorm : sqrt(a);
+        }
+        if (!isfinite(rel)) { status = CNV_NONFINITE; break; }
+        if (rel <= rtol) { status = CNV_OK; break; }
+        if (outer >= max_outer) break;
+        for (int x = tid; x < 2 * plane; x += nt) smem[x] = 0.0f;
+        __syncthreads();
+        for (int e = 0; e < epochs; ++e) {
+            for (int h = 1; h <= 2 * kStripSweeps; ++h) {
+                const int c = (h - 1) & 1, grow = kStripHalo - h;
+                const int lo = R0 - grow > 1 ? R0 - grow : 1;
+                const int hi = R1 + grow < n - 1 ? R1 + grow : n - 1;
+                strip_half_sweep(es[c], es[c ^ 1], C.rq[c], sr0, sp, P, lo, hi, n, c, wxf, wyf, betaf);
+                __syncthreads();
+            }
+            if (e + 1 < epochs) {
+                // border rows -> exchange copy of this epoch's parity; halo rows <- neighbours'
+                // (split columns m < (n+1)/2 hold every interior cell; both pitches cover them)
+                float* const* X = (e & 1) ? C.ex1 : C.e;
+                const int mw = (n + 1) / 2;
+                for (int x = tid; x < 2 * kStripHalo * mw; x += nt) {
+                    const int k = x / mw, m = x - k * mw;
+                    const int i = k < kStripHalo ? R0 + k : R1 - 2 * kStripHalo + k;
+                    if (i < 1 || i > n - 2 || i < R0 || i >= R1) continue;
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        const int j = 2 * m + ((i + c) & 1);
+                        if (j >= 1 && j <= n - 2) X[c][(size_t)i * P + m] = es[c][(i - sr0) * sp + m];
+                    }
+                }
+                if (!group_barrier(gs, gen, g, abort, s_ok)) return CNV_TIMEOUT;
+                for (int x = tid; x < 2 * kStripHalo * mw; x += nt) {
+                    const int k = x / mw, m = x - k * mw;
+                    const int i = k < kStripHalo ? R0 - kStripHalo + k : R1 + (k - kStripHalo);
+                    if (i < 1 || i > n - 2 || i < sr0 || i >= sr1) continue;
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        const int j = 2 * m + ((i + c) & 1);
+                        if (j >= 1 && j <= n - 2) es[c][(i - sr0) * sp + m] = __ldcg(X[c] + (size_t)i * P + m);
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        sweeps += C.inner;
+        // psi += e (FP64) on the strip's own interior cells
+        for (int x = tid; x < (ri1 - ri0) * (n - 2); x += nt) {
+            const int i = ri0 + x / (n - 2), j = 1 + (x - (x / (n - 2)) * (n - 2));
+            const int c = (i + j) & 1;
+            C.psi[c][(size_t)i * P + (j >> 1)] += (double)es[c][(i - sr0) * sp + (j >> 1)];
+        }
+        if (!group_barrier(gs, gen, g, abort, s_ok)) return CNV_TIMEOUT;
+    }
+
+    // velocity u = DY psi, v = -(DX psi) on the strip's rows (src/main.c:366-383)
+    auto PS = [&](int y, int x) { return LD(C.psi[(y + x) & 1] + (size_t)y * P + (x >> 1)); };
+    for (int x = tid; x < rows * n; x += nt) {
+        const int i = R0 + x / n, j = x - (x / n) * n;
+        const size_t k = (size_t)i * n + j;
+        C.u[k] = along_i(B->d1y, n, i, j, PS);
+        C.v[k] = -along_j(B->d1x, n, i, j, PS);
+        C.psi_rm[k] = PS(i, j);
+    }
+    if (!group_barrier(gs, gen, g, abort, s_ok)) return CNV_TIMEOUT;
+    // continuity DX u + DY v on the strip's rows, max and min over the group (src/main.c:387-408)
+    double mx = -DBL_MAX, mn = DBL_MAX;
+    auto Uf = [&](int y, int x) { return LD(C.u + (size_t)y * n + x); };
+    auto Vf = [&](int y, int x) { return LD(C.v + (size_t)y * n + x); };
+    for (int x = tid; x < rows * n; x += nt) {
+        const int i = R0 + x / n, j = x - (x / n) * n;
+        const double cv = dadd(along_j(B->d1x, n, i, j, Uf), along_i(B->d1y, n, i, j, Vf));
+        mx = cv > mx ? cv : mx;
+        mn = cv < mn ? cv : mn;
+    }
+    block_minmax(mx, mn, s_red);
+    if (tid == 0) {
+        gs->cont[r][0] = mx;
+        gs->cont[r][1] = mn;
+    }
+    if (!group_barrier(gs, gen, g, abort, s_ok)) return CNV_TIMEOUT;
+    mx = -DBL_MAX;
+    mn = DBL_MAX;
+    for (int k = 0; k < g; ++k) {
+        const double a = __ldcg(&gs->cont[k][0]), b2 = __ldcg(&gs->cont[k][1]);
+        mx = a > mx ? a : mx;
+        mn = b2 < mn ? b2 : mn;
+    }
+    rec.iters = outer;
+    rec.status = status;
+    rec.err = rel;
+    rec.cont_max = mx;
+    rec.cont_min = mn;
+    return status;
+}
+
 __global__ void __launch_bounds__(kMaxBatchThreads) k_batch(BatchLaunch L) {
     extern __shared__ float smem[];
     __shared__ double s_red[64];
-    __shared__ int s_job;
+    __shared__ int s_ok;
     const int nsteps = *L.nsteps;
-    for (;;) {
-        if (threadIdx.x == 0) s_job = atomicAdd(L.queue, 1);
-        __syncthreads();
-        const int job = s_job;
-        __syncthreads();
-        if (job >= L.count) break;
-        CavityDesc& C = L.cav[L.order[job]];
-        if (threadIdx.x == 0) {
-            C.sweeps = 0;
-            C.steps_done = 0;
+    for (int e = L.sched_off[blockIdx.x]; e < L.sched_off[blockIdx.x + 1]; ++e) {
+        const SchedEntry J = L.sched[e];
+        CavityDesc& C = L.cav[J.cav];
+        if (J.group == 1) {
+            if (threadIdx.x == 0) {
+                C.sweeps = 0;
+                C.steps_done = 0;
+            }
+            __syncthreads();
+            for (int t = 0; t < nsteps; ++t) {
+                const int st = batch_step(C, smem, L.max_outer, L.rtol, L.warm != 0, s_red);
+                if (threadIdx.x == 0) C.steps_done = t + 1;
+                if (st != CNV_OK) break;
+            }
+            __syncthreads();
+            continue;
+        }
+        // a strip of a cavity shared by J.group blocks; the descriptor's cur, sweeps, record and
+        // step count are written once, by rank 0, when the job ends
+        GroupSync* gs = L.gsync + J.cav;
+        unsigned gen = 0;
+        int cur = C.cur;
+        long long sweeps = 0;
+        int done = 0;
+        StepRecord rec{};
+        for (int t = 0; t < nsteps; ++t) {
+            const int st = group_step(C, cur, J.rank, J.group, smem, L.max_outer, L.rtol, L.warm != 0, s_red, gs, gen,
+                                      L.abort, &s_ok, sweeps, rec);
+            if (st == CNV_TIMEOUT) {
+                rec.status = CNV_TIMEOUT;
+                break;
+            }
+            cur ^= 1;
+            done = t + 1;
+            if (st != CNV_OK) break;
         }
         __syncthreads();
-        for (int t = 0; t < nsteps; ++t) {
-            const int st = batch_step(C, smem, L.max_outer, L.rtol, L.warm != 0, s_red);
-            if (threadIdx.x == 0) C.steps_done = t + 1;
-            if (st != CNV_OK) break;
+        if (J.rank == 0 && threadIdx.x == 0) {
+            C.cur = cur;
+            C.sweeps = sweeps;
+            C.steps_done = done;
+            C.last = rec;
         }
         __syncthreads();
     }
@@ -293,8 +618,12 @@ struct cnv_batch {
     FdBands* bands = nullptr;
     void* arena = nullptr;
     size_t arena_bytes = 0;
-    int* order = nullptr;
-    int* queue = nullptr;
+    SchedEntry* sched = nullptr;   // job lists (device)
+    int* sched_off = nullptr;      // per block offsets into sched (device)
+    GroupSync* gsync = nullptr;    // per cavity (device)
+    int* abort = nullptr;          // group-wait failure flag (device)
+    int split = 1;                 // strips per cavity beyond what shared memory needs
+    int split_min_n = 256;         // ... for cavities of at least this many points per side
     int* nsteps = nullptr;
     int threads = 1024;
     int blocks = 0;
@@ -306,6 +635,7 @@ struct cnv_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0;
     long long cells = 0;
+    double makespan_us = 0;        // the schedule's estimated step time
     std::string err;
 };
 
@@ -329,7 +659,42 @@ inline unsigned long long mix64(unsigned long long z) {
     return z ^ (z >> 31);
 }
 
-double cost_of(int n) { return (double)n * n * n; }  // ~ sweeps (n) x cells (n^2)
+// Row strips a cavity needs so that one strip's FP32 correction (plus halo rows) fits a block's
+// shared memory: 1 if the whole cavity's correction fits, else the smallest power of two that
+// does (strips at least 2 halos high); then `split` times more for cavities of at least min_n
+// points. 0 if no decomposition fits.
+int group_size(int n, int smem_bytes, int split, int min_n) {
+    const size_t sp = (size_t)(n + 1) / 2 + 1;
+    int g = 0;
+    if (2 * (size_t)n * sp * 4 <= (size_t)smem_bytes) {
+        g = 1;
+    } else {
+        for (int t = 2; t <= kMaxGroup; t *= 2) {
+            const size_t rows = (size_t)(n + t - 1) / t + 2 * kStripHalo;
+            if (n / t >= 2 * kStripHalo && 2 * rows * sp * 4 <= (size_t)smem_bytes) {
+                g = t;
+                break;
+            }
+        }
+        if (!g) return 0;
+    }
+    if (n >= min_n)
+        while (split > 1 && g * 2 <= kMaxGroup && n / (g * 2) >= 2 * kStripHalo) {
+            g *= 2;
+            split /= 2;
+        }
+    return g;
+}
+
+// Estimated device time of one step of an n x n cavity on g blocks (microseconds): about 4n FP32
+// sweeps over n^2 cells at the measured per-SM rates (3.9 k cells/us with the correction in
+// shared memory, 1.5 k from L2), with the halo rows of a strip, plus the FP64 passes.
+double step_cost(int n, int g, int smem_mode) {
+    const double cells = (double)n * n;
+    const double rate = (g > 1 || smem_mode >= 1) ? 3.9e3 : 1.5e3;
+    const double halo = g > 1 ? ((double)n / g + 2 * kStripHalo) / ((double)n / g) : 1.0;
+    return (4.0 * n * cells / rate * halo + 0.061 * cells) / g;
+}
 
 int build_graph(cnv_batch* b) {
     if (b->graph) {
@@ -338,8 +703,10 @@ int build_graph(cnv_batch* b) {
     }
     BatchLaunch L{};
     L.cav = b->desc;
-    L.order = b->order;
-    L.queue = b->queue;
+    L.sched = b->sched;
+    L.sched_off = b->sched_off;
+    L.gsync = b->gsync;
+    L.abort = b->abort;
     L.nsteps = b->nsteps;
     L.count = b->count;
     L.max_outer = b->max_outer;
@@ -349,9 +716,21 @@ int build_graph(cnv_batch* b) {
     BCUDA(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem_bytes));
     cudaGraph_t g = nullptr;
     BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    cudaMemsetAsync(b->queue, 0, sizeof(int), b->stream);
-    k_batch<<<b->blocks, b->threads, b->smem_bytes, b->stream>>>(L);
-    const cudaError_t le = cudaGetLastError();
+    cudaMemsetAsync(b->gsync, 0, sizeof(GroupSync) * b->count, b->stream);
+    cudaMemsetAsync(b->abort, 0, sizeof(int), b->stream);
+    // cooperative: the blocks of a group wait for one another, so all must be resident
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(b->blocks);
+    cfg.blockDim = dim3(b->threads);
+    cfg.dynamicSmemBytes = b->smem_bytes;
+    cfg.stream = b->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {&L};
+    const cudaError_t le = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_batch), args);
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (le != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -364,7 +743,60 @@ int build_graph(cnv_batch* b) {
     return CNV_OK;
 }
 
-// Launch shape: threads per block and blocks per SM; shared memory as the SM allows.
+// Job lists: cavities largest estimated cost first, each on the `group` blocks that become free
+// first; every block's list in start-time order (so groups meet in one global order).
+int build_schedule(cnv_batch* b) {
+    const int nb = b->blocks;
+    std::vector<int> idx(b->count);
+    std::iota(idx.begin(), idx.end(), 0);
+    std::vector<double> cost(b->count);
+    for (int k = 0; k < b->count; ++k) {
+        const CavityDesc& d = b->host_desc[k];
+        cost[k] = step_cost(d.n, d.group, d.smem_mode);
+    }
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int c) { return cost[a] > cost[c]; });
+    std::vector<double> avail(nb, 0.0);
+    struct Placed {
+        double start;
+        int cav, rank, group;
+    };
+    std::vector<std::vector<Placed>> lists(nb);
+    std::vector<int> blocks(nb);
+    for (int k : idx) {
+        const int g = b->host_desc[k].group;
+        if (g > nb) return bfail(CNV_BAD_ARG, "a cavity needs more blocks than the device runs at once");
+        std::iota(blocks.begin(), blocks.end(), 0);
+        std::stable_sort(blocks.begin(), blocks.end(), [&](int a, int c) { return avail[a] < avail[c]; });
+        double start = 0.0;
+        for (int r = 0; r < g; ++r) start = std::max(start, avail[blocks[r]]);
+        for (int r = 0; r < g; ++r) {
+            lists[blocks[r]].push_back(Placed{start, k, r, g});
+            avail[blocks[r]] = start + cost[k];
+        }
+    }
+    std::vector<SchedEntry> flat;
+    std::vector<int> off(nb + 1, 0);
+    for (int q = 0; q < nb; ++q) {
+        // start times are non-decreasing within a list already; keep that order
+        off[q] = (int)flat.size();
+        for (const Placed& e : lists[q]) flat.push_back(SchedEntry{e.cav, e.rank, e.group, 0});
+    }
+    off[nb] = (int)flat.size();
+    if (b->sched) cudaFree(b->sched);
+    if (b->sched_off) cudaFree(b->sched_off);
+    b->sched = nullptr;
+    b->sched_off = nullptr;
+    BCUDA(cudaMalloc(&b->sched, sizeof(SchedEntry) * std::max<size_t>(flat.size(), 1)));
+    BCUDA(cudaMalloc(&b->sched_off, sizeof(int) * (nb + 1)));
+    if (!flat.empty())
+        BCUDA(cudaMemcpy(b->sched, flat.data(), sizeof(SchedEntry) * flat.size(), cudaMemcpyHostToDevice));
+    BCUDA(cudaMemcpy(b->sched_off, off.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice));
+    b->makespan_us = *std::max_element(avail.begin(), avail.end());
+    return CNV_OK;
+}
+
+// Launch shape: threads per block and blocks per SM; shared memory as the SM allows; the strip
+// decomposition and the job lists for it.
 int set_shape(cnv_batch* b, int threads, int per_sm) {
     int dev_smem = 0;
     BCUDA(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, b->device));
@@ -377,12 +809,17 @@ int set_shape(cnv_batch* b, int threads, int per_sm) {
     BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch, threads, b->smem_bytes));
     if (occ < 1) return bfail(CNV_CUDA_ERROR, "batched kernel does not fit on an SM");
     b->blocks = std::min(occ, per_sm) * b->sms;
-    // per-cavity placement of the FP32 correction for this shared-memory size
+    // per-cavity placement of the FP32 correction for this shared-memory size, and row strips
     for (auto& d : b->host_desc) {
         const size_t plane = (size_t)d.n * d.spitch * 4;
         d.smem_mode = 4 * plane <= (size_t)b->smem_bytes ? 2 : 2 * plane <= (size_t)b->smem_bytes ? 1 : 0;
+        d.group = group_size(d.n, b->smem_bytes, b->split, b->split_min_n);
+        if (d.group == 0) d.group = 1;  // no strip decomposition fits: one block, correction in L2
+        if (d.group > 1) d.smem_mode = 1;
     }
     BCUDA(cudaMemcpy(b->desc, b->host_desc.data(), sizeof(CavityDesc) * b->count, cudaMemcpyHostToDevice));
+    const int rc = build_schedule(b);
+    if (rc != CNV_OK) return rc;
     return build_graph(b);
 }
 
@@ -456,7 +893,7 @@ int cnv_batch_create(const cnv_config* base, int count, const cnv_cavity_spec* s
         return cleanup(CNV_CUDA_ERROR, "stream/event creation failed");
 
     // arena: per cavity w[2], u, v, psi_rm (n*n doubles each), psi/g split (2 x n*pitch doubles
-    // each), e/rq split (2 x n*pitch floats each)
+    // each), e/rq/ex1 split (2 x n*pitch floats each)
     std::vector<size_t> offs(count);
     size_t total = 0;
     auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -465,15 +902,15 @@ int cnv_batch_create(const cnv_config* base, int count, const cnv_cavity_spec* s
         const int n = specs[k].n;
         const int pitch = ((n + 1) / 2 + 31) / 32 * 32;
         offs[k] = total;
-        total += align(5 * (size_t)n * n * 8) + align(4 * (size_t)n * pitch * 8) + align(4 * (size_t)n * pitch * 4);
+        total += align(5 * (size_t)n * n * 8) + align(4 * (size_t)n * pitch * 8) + align(6 * (size_t)n * pitch * 4);
         b->cells += (long long)n * n;
     }
     b->arena_bytes = total;
     if (cudaMalloc(&b->arena, total) != cudaSuccess) return cleanup(CNV_CUDA_ERROR, "arena allocation failed");
     if (cudaMalloc(&b->desc, sizeof(CavityDesc) * count) != cudaSuccess ||
         cudaMalloc(&b->bands, sizeof(FdBands) * count) != cudaSuccess ||
-        cudaMalloc(&b->order, sizeof(int) * count) != cudaSuccess ||
-        cudaMalloc(&b->queue, sizeof(int)) != cudaSuccess || cudaMalloc(&b->nsteps, sizeof(int)) != cudaSuccess)
+        cudaMalloc(&b->gsync, sizeof(GroupSync) * count) != cudaSuccess ||
+        cudaMalloc(&b->abort, sizeof(int)) != cudaSuccess || cudaMalloc(&b->nsteps, sizeof(int)) != cudaSuccess)
         return cleanup(CNV_CUDA_ERROR, "descriptor allocation failed");
 
     std::vector<FdBands> hb(count);
@@ -525,13 +962,11 @@ int cnv_batch_create(const cnv_config* base, int count, const cnv_cavity_spec* s
         d.e[1] = f32 + (size_t)n * pitch;
         d.rq[0] = f32 + 2 * (size_t)n * pitch;
         d.rq[1] = f32 + 3 * (size_t)n * pitch;
+        d.ex1[0] = f32 + 4 * (size_t)n * pitch;
+        d.ex1[1] = f32 + 5 * (size_t)n * pitch;
+        d.group = 1;
     }
-    // largest estimated cost first
-    std::vector<int> order(count);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return cost_of(specs[a].n) > cost_of(specs[c].n); });
-    if (cudaMemcpy(b->bands, hb.data(), sizeof(FdBands) * count, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(b->order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice) != cudaSuccess)
+    if (cudaMemcpy(b->bands, hb.data(), sizeof(FdBands) * count, cudaMemcpyHostToDevice) != cudaSuccess)
         return cleanup(CNV_CUDA_ERROR, "descriptor upload failed");
     int rc = reset_fields(b);
     if (rc == CNV_OK) rc = set_shape(b, 1024, 1);
@@ -547,7 +982,8 @@ void cnv_batch_destroy(cnv_batch* b) {
     if (!b) return;
     cudaSetDevice(b->device);
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    for (void* p : {(void*)b->arena, (void*)b->desc, (void*)b->bands, (void*)b->order, (void*)b->queue, (void*)b->nsteps})
+    for (void* p : {(void*)b->arena, (void*)b->desc, (void*)b->bands, (void*)b->sched, (void*)b->sched_off,
+                    (void*)b->gsync, (void*)b->abort, (void*)b->nsteps})
         if (p) cudaFree(p);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -564,27 +1000,49 @@ int cnv_batch_reset(cnv_batch* b) {
 int cnv_batch_tune(cnv_batch* b, int* threads_out, int* blocks_per_sm_out) {
     if (!b) return bfail(CNV_BAD_ARG, "null batch");
     BCUDA(cudaSetDevice(b->device));
-    // candidates: (threads, blocks per SM); each timed for one step from the initial state
-    const int cand[][2] = {{1024, 1}, {512, 1}, {512, 2}, {256, 2}};
+    // candidates: row-strip decompositions (strips only where shared memory needs them, or 2x or
+    // 4x as many for the largest cavities), each timed for one step from the initial state, on
+    // one block of 1024 threads per SM (the shared-memory tiles need the whole SM)
+    const int cand[][2] = {{1, 256}, {2, 256}, {4, 256}, {2, 192}};
     double best = 1e300;
-    int bt = 1024, bp = 1;
+    int bs = 1, bm = 256;
     for (const auto& c : cand) {
-        int rc = set_shape(b, c[0], c[1]);
+        b->split = c[0];
+        b->split_min_n = c[1];
+        int rc = set_shape(b, 1024, 1);
         if (rc != CNV_OK) continue;
         rc = reset_fields(b);
         if (rc == CNV_OK) rc = run(b, 1);
         if (rc != CNV_OK) return rc;
         if (b->last_ms < best) {
             best = b->last_ms;
-            bt = c[0];
-            bp = c[1];
+            bs = c[0];
+            bm = c[1];
         }
     }
-    int rc = set_shape(b, bt, bp);
+    b->split = bs;
+    b->split_min_n = bm;
+    int rc = set_shape(b, 1024, 1);
     if (rc == CNV_OK) rc = reset_fields(b);
-    if (threads_out) *threads_out = bt;
-    if (blocks_per_sm_out) *blocks_per_sm_out = bp;
+    if (threads_out) *threads_out = b->threads;
+    if (blocks_per_sm_out) *blocks_per_sm_out = 1;
     return rc;
+}
+
+int cnv_batch_split(cnv_batch* b, int factor, int min_n) {
+    if (!b || factor < 1 || factor > kMaxGroup || min_n < 1) return bfail(CNV_BAD_ARG, "bad batch or split factor");
+    BCUDA(cudaSetDevice(b->device));
+    b->split = factor;
+    b->split_min_n = min_n;
+    int rc = set_shape(b, 1024, 1);
+    if (rc == CNV_OK) rc = reset_fields(b);
+    return rc;
+}
+
+int cnv_batch_groups(cnv_batch* b, int* groups) {
+    if (!b || !groups) return bfail(CNV_BAD_ARG, "null argument");
+    for (int k = 0; k < b->count; ++k) groups[k] = b->host_desc[k].group;
+    return CNV_OK;
 }
 
 int cnv_batch_step(cnv_batch* b, int nsteps, cnv_step_info* last) {
@@ -592,7 +1050,10 @@ int cnv_batch_step(cnv_batch* b, int nsteps, cnv_step_info* last) {
     BCUDA(cudaSetDevice(b->device));
     int rc = run(b, nsteps);
     if (rc != CNV_OK) return rc;
+    int aborted = 0;
+    BCUDA(cudaMemcpy(&aborted, b->abort, sizeof(int), cudaMemcpyDeviceToHost));
     BCUDA(cudaMemcpy(b->host_desc.data(), b->desc, sizeof(CavityDesc) * b->count, cudaMemcpyDeviceToHost));
+    if (aborted) return bfail(CNV_TIMEOUT, "a wait between the blocks of a cavity's group gave up");
     int status = CNV_OK;
     for (int k = 0; k < b->count; ++k) {
         const CavityDesc& d = b->host_desc[k];

@@ -186,11 +186,13 @@ int cnv_poisson_noalloc(const double *f, double *psi, int n, double dx, double d
                         int *iters, double *err, void *stream);
 
 /* ---------------------------------------------------------------------------------------
- * Batched form: many independent cavities (uneven grid size, Re, lid speed) advanced by one
- * persistent launch (captured in a CUDA graph). Each cavity runs the step of cnv_step with the
- * mixed-precision Poisson solve (FP32 red-black SOR inside FP64 defect correction to relative
- * residual base->mixed_rtol, default 1e-10). No counterpart in the reference, which runs one
- * cavity per process.
+ * Batched form: many independent cavities (uneven grid size, Re and lid speed) advanced by one
+ * persistent cooperative launch (captured in a CUDA graph). Each cavity runs the step of cnv_step
+ * with the mixed-precision Poisson solve (FP32 red-black SOR inside FP64 defect correction to
+ * relative residual base->mixed_rtol, default 1e-10). A cavity whose FP32 correction does not
+ * fit one block's shared memory is split into row strips run by a group of blocks; the host
+ * schedules the cavities (largest first) onto the blocks. No counterpart in the reference, which
+ * runs one cavity per process.
  * ------------------------------------------------------------------------------------- */
 typedef struct cnv_cavity_spec {
     int n;       /* grid points per side */
@@ -209,9 +211,16 @@ int cnv_batch_specs(int count, unsigned long long seed, cnv_cavity_spec *out);
 int cnv_batch_create(const cnv_config *base, int count, const cnv_cavity_spec *specs, cnv_batch **out);
 void cnv_batch_destroy(cnv_batch *b);
 int cnv_batch_reset(cnv_batch *b);
-/* Time one step of each candidate launch shape from the initial state, keep the fastest, and
- * reset the fields. threads / blocks_per_sm may be NULL. */
+/* Time one step of each candidate decomposition (row strips only where shared memory needs
+ * them, or 2x / 4x as many for the largest cavities) from the initial state, keep the fastest,
+ * and reset the fields. Reports the launch shape (threads per block, blocks per SM); either
+ * pointer may be NULL. */
 int cnv_batch_tune(cnv_batch *b, int *threads, int *blocks_per_sm);
+/* Use factor times more row strips than shared memory needs for cavities of at least min_n
+ * points per side (factor 1: only as needed), rebuild the schedule and reset the fields. */
+int cnv_batch_split(cnv_batch *b, int factor, int min_n);
+/* Blocks (row strips) of each cavity under the current decomposition (count entries). */
+int cnv_batch_groups(cnv_batch *b, int *groups);
 /* Advance every cavity nsteps steps in one launch; last (count records or NULL) receives each
  * cavity's last step. */
 int cnv_batch_step(cnv_batch *b, int nsteps, cnv_step_info *last);

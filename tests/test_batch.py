@@ -106,3 +106,49 @@ def test_warm_batch_equals_warm_single_cavity_runs(cnv):
         assert last[k]["iters"] == steps[-1]["iters"]
         for name, a, b in zip("w u v psi".split(), fields[k], single):
             assert np.max(np.abs(a - b)) <= SAME_SCHEME_TOL * np.max(np.abs(b)), (k, name)
+
+
+def _single_mixed(cnv, sp, nsteps, **kw):
+    cfg = cnv.default_config(nx=sp["n"], ny=sp["n"], Re=sp["Re"], u4=sp["lid"],
+                             dt=_stable_dt(sp["n"], sp["Re"], sp["lid"]), precision=cnv.PREC_MIXED,
+                             mixed_rtol=1e-10, **kw)
+    with cnv.Cavity(cfg) as cav:
+        _, steps = cav.step(nsteps)
+        return steps, cav.get_fields()
+
+
+@pytest.mark.gpu
+def test_row_strip_groups_equal_single_cavity_runs(cnv):
+    """Cavities split into 2 or 4 row strips (forced on small grids) give the single-cavity
+    mixed run's fields: the strips' halo exchange reproduces global red-black sweeps."""
+    base = cnv.default_config(mixed_rtol=1e-10)
+    nsteps = 3
+    with cnv.Batch(base, SPECS) as bt:
+        bt.split(4, 1)
+        groups = bt.groups()
+        rc, last = bt.step(nsteps)
+        fields = [bt.get_fields(k) for k in range(len(SPECS))]
+    assert rc == 0
+    assert groups == [4, 2, 4, 2, 4]
+    for k, sp in enumerate(SPECS):
+        steps, single = _single_mixed(cnv, sp, nsteps)
+        assert last[k]["iters"] == steps[-1]["iters"], k
+        for name, a, b in zip("w u v psi".split(), fields[k], single):
+            assert np.max(np.abs(a - b)) <= SAME_SCHEME_TOL * np.max(np.abs(b)), (k, name)
+
+
+@pytest.mark.gpu
+def test_large_cavities_on_their_default_strips(cnv):
+    specs = [dict(n=384, Re=1500.0, lid=1.2), dict(n=256, Re=300.0, lid=0.7), dict(n=192, Re=900.0, lid=1.0)]
+    base = cnv.default_config(mixed_rtol=1e-10)
+    nsteps = 2
+    with cnv.Batch(base, specs) as bt:
+        groups = bt.groups()
+        rc, last = bt.step(nsteps)
+        fields = [bt.get_fields(k) for k in range(len(specs))]
+    assert rc == 0 and groups[0] > 1 and groups[1] > 1
+    for k, sp in enumerate(specs):
+        steps, single = _single_mixed(cnv, sp, nsteps)
+        assert last[k]["iters"] == steps[-1]["iters"], k
+        for name, a, b in zip("w u v psi".split(), fields[k], single):
+            assert np.max(np.abs(a - b)) <= SAME_SCHEME_TOL * np.max(np.abs(b)), (k, name)
