@@ -574,11 +574,13 @@ def only(args):
 
     cnvpy.load()
     out = {}
-    for name in args.only.split(","):
+    for item in args.only.split(","):
+        name, _, size = item.partition("@")  # e.g. fp64@512: that form on a 512^2 cavity
         t0 = time.perf_counter()
         if name in ("fp64", "fp64_fma", "mixed", "direct"):
             prec, ptype, _ = FORMS[name]
-            run_device(cnvpy, workload(1024), 0, 1, 0, lambda: None, precision=prec, poisson_type=ptype)
+            run_device(cnvpy, workload(int(size) if size else 1024), 0, 1, 0, lambda: None, precision=prec,
+                       poisson_type=ptype)
         elif name == "batched":
             with cnvpy.Batch(cnvpy.default_config(mixed_rtol=1e-10), cnvpy.batch_specs(256, seed=0)) as bt:
                 bt.step(1)
@@ -590,7 +592,7 @@ def only(args):
                 adj.enstrophy_gradient(cnvpy.noise_field(n, seed=2025, sigma=1.0, passes=16), 1.0, 20)
         else:
             raise SystemExit(f"unknown form {name}")
-        out[name] = round(time.perf_counter() - t0, 3)
+        out[item] = round(time.perf_counter() - t0, 3)
     print(json.dumps({"only": out, "unit": "s (wall, first call)"}), flush=True)
 
 
@@ -606,8 +608,8 @@ def main():
     ap.add_argument("--form", choices=["fp64", "fp64_fma", "mixed"], default="fp64",
                     help="form measured for the headline value")
     ap.add_argument("--only", default=None,
-                    help="comma list of fp64,fp64_fma,mixed,direct,batched,adjoint: run one small case of each "
-                         "(for profilers) and exit")
+                    help="comma list of fp64,fp64_fma,mixed,direct,batched,adjoint (fp64@512: on a 512^2 "
+                         "cavity): run one small case of each (for profilers) and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least 3 untimed warm-up steps
     if args.only:
