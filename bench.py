@@ -82,7 +82,8 @@ class Dist:
 
             backend = "nccl" if torch.cuda.is_available() else "gloo"
             td.init_process_group(backend)
-            self.td, self.torch, self.device = td, torch, device
+            self.td, self.torch = td, torch
+            self.device = f"cuda:{device}" if backend == "nccl" else "cpu"
 
     def barrier(self):
         if self.ws > 1:
@@ -91,7 +92,7 @@ class Dist:
     def max(self, x: float) -> float:
         if self.ws == 1:
             return x
-        t = self.torch.tensor([x], dtype=self.torch.float64, device=f"cuda:{self.device}")
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.device)
         self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
         return float(t.item())
 
@@ -602,7 +603,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--n", type=int, default=1024, help=argparse.SUPPRESS)
+    ap.add_argument("--grid", dest="n", type=int, default=1024, help=argparse.SUPPRESS)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
     ap.add_argument("--skip-forms", action="store_true", help="omit the extra precision/batch forms")
     ap.add_argument("--form", choices=["fp64", "fp64_fma", "mixed"], default="fp64",
