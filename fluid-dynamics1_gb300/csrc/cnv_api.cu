@@ -824,8 +824,10 @@ int cnv_poisson_device(cnv_state* s, const double* f, double* psi_out, int* iter
     if (rc != CNV_OK) return rc;
     CNV_CUDA(launch_to_split(f, s->rhs[0], s->rhs[1], s->sa, s->stream));
     CNV_CUDA(cudaEventRecord(s->ev0, s->stream));
+    CNV_CUDA(cudaEventRecord(s->evp0, s->stream));
     rc = enqueue_poisson(s, f, -s->sa.c4, false);
     if (rc != CNV_OK) return rc;
+    CNV_CUDA(cudaEventRecord(s->evp1, s->stream));
     CNV_CUDA(cudaEventRecord(s->ev1, s->stream));
     CNV_CUDA(launch_from_split(s->sor[0], s->sor[1], psi_out, s->n, s->pitch, s->stream));
     Ctrl h{};

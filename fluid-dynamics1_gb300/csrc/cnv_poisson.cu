@@ -11,17 +11,28 @@
 // block per SM (or two), so every SM gets the same work. psi is kept in two copies ("sets") of
 // the red/black split layout: sweep k reads set (k-1)&1 and writes set k&1, so the state of
 // sweep k stays intact while sweep k+1 runs. A tile's interior cells depend only on the tile's
-// own data; its frame (first/last row/column next to another tile) reads the neighbours'. Each
-// half-sweep waits for the four neighbours' progress flags (one thread per neighbour, in
-// parallel), updates the frame, publishes its own flag at once, and then updates the interior
-// while the neighbours catch up. There is no grid-wide barrier.
+// own data; its frame (first/last row/column next to another tile) reads the neighbours'.
+//
+// Warp roles. Fifteen warps update cells; the sixteenth (the signal warp) does all inter-block
+// work: it polls the four neighbours' progress flags, raises this block's flag once the frame
+// is written (fence + release store), adds the block's share of the stop norm to the global
+// accumulator and runs the stop test. The two sides meet only at named barriers that the
+// cell-update warps pass through without waiting for any fence or poll (bar.arrive where they
+// hand something over, bar.sync only where they need the signal warp's answer, which it
+// prepares ahead). In each half-sweep the first four warps wait for the neighbours' frames
+// (barrier GO), update this colour's frame and hand it to the signal warp (PUB); every
+// cell-update warp then takes 32-cell chunks of the interior from a shared counter, so the
+// frame's latency is covered by the other warps' interior work and the FP64 pipe never idles
+// on a block-wide barrier. There is no grid-wide barrier.
 //
 // Stop test. Each block adds its partial sum of |dpsi| to a 128-bit fixed-point accumulator
 // (scale 2^80, kept as four 32-bit chunks in 64-bit counters: exact integer adds with no carry,
-// so the total is independent of arrival order) in a ring of 8 slots, and counts itself in. A block checks e_{k-2} at the start of sweep k, when it is
-// long complete; if e_{k-2} < tol every block stops before overwriting set (k-2)&1, which holds
-// the answer. The extra sweep k-1 is discarded. Every wait is bounded by a timeout and by the
-// abort flag, and records CNV_TIMEOUT instead of hanging.
+// so the total is independent of arrival order) in a ring of 8 slots, and counts itself in. The
+// signal warp checks e_{k-2} while the other warps finish sweep k-1 and posts the verdict at
+// barrier DEC before sweep k; if e_{k-2} < tol every block stops before overwriting set
+// (k-2)&1, which holds the answer. The extra sweep k-1 is discarded. Every wait of the signal
+// warp is bounded by a timeout and by the abort flag, and records CNV_TIMEOUT instead of
+// hanging; it then still passes every barrier, so the block always reaches its end.
 //
 // Arithmetic. Arith::kExact reproduces the reference's point update bit for bit: in general with
 // the full operation sequence of src/poisson.c:247 (division by 2*(dx^2+dy^2) exact when that is
@@ -43,7 +54,28 @@ namespace cnv {
 namespace {
 
 constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+constexpr int kCellWarps = kWarps - 1;          // warps 0..14 update cells
+constexpr int kCellThreads = kCellWarps * 32;
+constexpr int kSignalWarp = kWarps - 1;         // warp 15: flags, norm, stop test
+constexpr int kFrameWarps = 4;                  // warps 0..3 also update the frame
+constexpr int kFrameThreads = kFrameWarps * 32;
 constexpr int kRing = 8;
+
+// Named barriers (0 is __syncthreads). DEC: the stop verdict for the next sweep (signal warp
+// arrives, cell warps wait). GO: the neighbours' frames are ready (signal warp arrives, frame
+// warps wait). PUB: this block's frame is written (frame warps arrive, signal warp waits). END:
+// the half-sweep is complete (cell warps only). NORM: the warps' norm partials are in shared
+// memory (cell warps arrive, signal warp waits).
+enum : int { kBarDec = 1, kBarGo = 2, kBarPub = 3, kBarEnd = 4, kBarNorm = 5 };
+constexpr int kGoThreads = kFrameThreads + 32;
+
+__device__ __forceinline__ void bar_sync(int id, int count) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(int id, int count) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
 
 struct Geometry {
     int n, pitch;
@@ -58,6 +90,16 @@ struct SyncState {
     unsigned int count[kRing];
     unsigned int nonfinite[kRing];
     unsigned int flag[2][kMaxSolverBlocks];  // [colour][block]: last sweep whose frame is written
+};
+
+// Block-shared state of the two warp roles.
+struct Shared {
+    unsigned long long part[2][kCellWarps][4];  // [sweep parity][warp] norm chunk sums
+    unsigned int pbig[2][kCellWarps];
+    unsigned int ctr[2];                        // interior chunk counters, by half-sweep parity
+    int stop[2];                                // verdict before sweep k, at [k & 1]
+    int status, conv_k;
+    double e_last;
 };
 
 struct Tile {
@@ -121,36 +163,105 @@ __device__ __forceinline__ void update_cell(const PoissonParams& p, int i, int j
     S_new[row + m] = point_update<A, KIND, FOLD>(p, up, dn, rt, lt, __ldg(rhs + row + m), old, acc);
 }
 
-// Interior cells of colour C (C = 2: both colours, Jacobi).
+// x / d for 0 <= x < 2^31 and 1 <= d, with m = 0xffffffff / d: the multiply-high estimate is
+// x/d or one less, and one correction step makes it exact.
+__device__ __forceinline__ int div_magic(int x, int d, unsigned m) {
+    int q = (int)__umulhi((unsigned)x, m);
+    if (x - q * d >= d) ++q;
+    return q;
+}
+
+// Interior cells of colour C (C = 2: both colours, Jacobi), in chunks taken from the block's
+// counter *ctr by whole warps until none is left. For one colour a chunk is 64 cells, two per
+// lane (x and x + 32, consecutive in a row: coalesced), loaded and updated together so that each
+// warp keeps two independent FP64 chains in flight; lanes past the region's end recompute the
+// region's first cell and store nothing.
 template <Arith A, int KIND, bool FOLD, int C>
-__device__ __forceinline__ void interior_pass(const PoissonParams& p, const Tile& t, const SweepPtrs& q,
-                                              NormAcc& acc) {
+__device__ __forceinline__ void interior_chunks(const PoissonParams& p, const Tile& t, const SweepPtrs& q,
+                                                NormAcc& acc, unsigned* ctr) {
     const int w = t.ci1 - t.ci0;
     const int h = t.ri1 - t.ri0;
     if (w <= 0 || h <= 0) return;
     const int wq = (w + 1) >> 1;
+    const unsigned mq = 0xffffffffu / (unsigned)wq;
     const int per_colour = h * wq;
-    const int total = (C == 2 ? 2 : 1) * per_colour;
-#pragma unroll 2
-    for (int x = threadIdx.x; x < total; x += kThreads) {
-        const int cc = C == 2 ? (x >= per_colour) : C;
-        const int xx = (C == 2 && cc) ? x - per_colour : x;
-        const int r = xx / wq;
-        const int i = t.ri0 + r;
-        const int j = t.ci0 + 2 * (xx - r * wq) + ((i + t.ci0 + cc) & 1);
-        if (j >= t.ci1) continue;
-        if (C == 2) {
-            if (cc)
-                update_cell<A, KIND, FOLD, false>(p, i, j, q.prev[1], q.next[1], q.oth[1], q.rhs[1], acc);
-            else
-                update_cell<A, KIND, FOLD, false>(p, i, j, q.prev[0], q.next[0], q.oth[0], q.rhs[0], acc);
-        } else {
-            update_cell<A, KIND, FOLD, false>(p, i, j, q.prev[C], q.next[C], q.oth[C], q.rhs[C], acc);
+    const int lane = threadIdx.x & 31;
+    if (C == 2) {
+        const int total = 2 * per_colour;
+        const unsigned nchunks = (unsigned)((total + 31) >> 5);
+        for (;;) {
+            unsigned c = 0;
+            if (lane == 0) c = atomicAdd(ctr, 1u);
+            c = __shfl_sync(0xffffffffu, c, 0);
+            if (c >= nchunks) break;
+            const int x = (int)c * 32 + lane;
+            if (x < total) {
+                const int cc = x >= per_colour;
+                const int xx = cc ? x - per_colour : x;
+                const int r = div_magic(xx, wq, mq);
+                const int i = t.ri0 + r;
+                const int j = t.ci0 + 2 * (xx - r * wq) + ((i + t.ci0 + cc) & 1);
+                if (j < t.ci1) {
+                    if (cc)
+                        update_cell<A, KIND, FOLD, false>(p, i, j, q.prev[1], q.next[1], q.oth[1], q.rhs[1], acc);
+                    else
+                        update_cell<A, KIND, FOLD, false>(p, i, j, q.prev[0], q.next[0], q.oth[0], q.rhs[0], acc);
+                }
+            }
+        }
+        return;
+    }
+    const double* __restrict__ Sp = q.prev[C];
+    double* __restrict__ Sn = q.next[C];
+    const double* __restrict__ O = q.oth[C];
+    const double* __restrict__ G = q.rhs[C];
+    const int pitch = p.pitch;
+    const unsigned nchunks = (unsigned)((per_colour + 63) >> 6);
+    for (;;) {
+        unsigned c = 0;
+        if (lane == 0) c = atomicAdd(ctr, 1u);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= nchunks) break;
+        size_t at[2];
+        int jl[2], jr[2];
+        bool ok[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int x = (int)c * 64 + u * 32 + lane;
+            const int xx = x < per_colour ? x : 0;
+            const int r = div_magic(xx, wq, mq);
+            const int i = t.ri0 + r;
+            const int j = t.ci0 + 2 * (xx - r * wq) + ((i + t.ci0 + C) & 1);
+            ok[u] = x < per_colour && j < t.ci1;
+            const int jj = ok[u] ? j : t.ci0;
+            const int ii = ok[u] ? i : t.ri0;
+            at[u] = (size_t)ii * pitch + (jj >> 1);
+            jl[u] = ((jj - 1) >> 1) - (jj >> 1);  // -1 or 0: the left neighbour's offset
+            jr[u] = ((jj + 1) >> 1) - (jj >> 1);  // 0 or +1
+        }
+        double old[2], up[2], dn[2], lt[2], rt[2], g[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            old[u] = Sp[at[u]];
+            up[u] = O[at[u] + pitch];
+            dn[u] = O[at[u] - pitch];
+            lt[u] = O[at[u] + jl[u]];
+            rt[u] = O[at[u] + jr[u]];
+            g[u] = __ldg(G + at[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const double nw = point_value<A, KIND, FOLD>(p, up[u], dn[u], rt[u], lt[u], g[u], old[u]);
+            if (ok[u]) {
+                Sn[at[u]] = nw;
+                norm_add(acc, nw, old[u]);
+            }
         }
     }
 }
 
-// Frame cells of colour C (C = 2: both colours): tile cells outside the interior region.
+// Frame cells of colour C (C = 2: both colours): tile cells outside the interior region, shared
+// out over the kFrameThreads threads of the frame warps.
 template <Arith A, int KIND, bool FOLD, int C>
 __device__ __forceinline__ void frame_pass(const PoissonParams& p, const Tile& t, const SweepPtrs& q,
                                            NormAcc& acc) {
@@ -160,7 +271,7 @@ __device__ __forceinline__ void frame_pass(const PoissonParams& p, const Tile& t
     const int mid = t.ri1 - t.ri0;
     const int n_rows = (top + bot) * W;
     const int total = n_rows + mid * (left + right);
-    for (int x = threadIdx.x; x < total; x += kThreads) {
+    for (int x = threadIdx.x; x < total; x += kFrameThreads) {
         int i, j;
         if (x < n_rows) {
             const int rr = x / W;
@@ -186,111 +297,71 @@ __device__ __forceinline__ void frame_pass(const PoissonParams& p, const Tile& t
     }
 }
 
-// Adds this block's share of e_k (chunk sums of the block in s_chunk[4], overflow flag in
-// s_big) to ring slot k % kRing. Called by one thread at a point where no block barrier waits
-// for it: the fence before the count stalls only that thread.
-__device__ __forceinline__ void contribute(SyncState* sy, int k, const unsigned long long* s_chunk,
-                                           unsigned int s_big) {
-    const int slot = k % kRing;
-    if (s_big) atomicOr(&sy->nonfinite[slot], 1u);
+// Signal warp, lane 0: adds this block's share of e_k (the cell warps' chunk sums of sweep k,
+// in sh.part[k & 1]) to ring slot k % kRing and counts the block in.
+__device__ __forceinline__ void contribute(SyncState* sy, int k, const Shared& sh) {
+    unsigned long long s[4] = {0, 0, 0, 0};
+    unsigned big = 0;
+    for (int w = 0; w < kCellWarps; ++w) {
 #pragma unroll
-    for (int w = 0; w < 4; ++w) atomicAdd(&sy->acc[slot][w], s_chunk[w]);
+        for (int c = 0; c < 4; ++c) s[c] += sh.part[k & 1][w][c];
+        big |= sh.pbig[k & 1][w];
+    }
+    const int slot = k % kRing;
+    if (big) atomicOr(&sy->nonfinite[slot], 1u);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) atomicAdd(&sy->acc[slot][c], s[c]);
     __threadfence();
     atomicAdd(&sy->count[slot], 1u);
 }
 
-// Threads 0..3 each wait for one neighbour's flag to reach `want` (in parallel); the block then
-// goes on together. Returns false if a wait gave up (timeout or abort).
-__device__ __forceinline__ bool neighbours_at(const unsigned* flags, const Tile& t, unsigned want, Ctrl* ctl,
-                                              long long timeout_ns, int* s_ok) {
-    if (threadIdx.x < 4) {
-        const int nb = t.nb[threadIdx.x];
-        s_ok[threadIdx.x] = nb < 0 ? 1 : (wait_geq(flags + nb, want, ctl, timeout_ns) ? 1 : 0);
-    }
-    __syncthreads();
-    const bool ok = s_ok[0] & s_ok[1] & s_ok[2] & s_ok[3];
-    return ok;
-}
-
-// After the frame pass: make this block's frame writes visible, then raise its flag. Only thread
-// 0 waits for the fence; the others go straight on to the interior pass.
-__device__ __forceinline__ void publish(unsigned* flag, unsigned value) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        st_release(flag, value);
-    }
-}
-
-template <Arith A, int KIND, bool FOLD>
-__global__ void __launch_bounds__(kThreads, 2) k_poisson(PoissonLaunch L) {
-    Ctrl* ctl = L.ctrl;
-    if (ctl->abort) return;
-    const PoissonParams p = L.p;
-    SyncState* sy = reinterpret_cast<SyncState*>(L.sync);
-    const Geometry geo{p.n, p.pitch, L.gx, L.gy};
-    const Tile t = make_tile(geo, blockIdx.x);
-    const int me = blockIdx.x;
-    __shared__ unsigned long long s_wchunk[kThreads / 32][4];
-    __shared__ unsigned long long s_chunk[4];
-    __shared__ unsigned int s_wbig[kThreads / 32];
-    __shared__ unsigned int s_big;
-    __shared__ int s_stop;    // 0 run on, 1 converged, 2 failure
-    __shared__ double s_e;
-    __shared__ int s_ok[4];
-
-    // two copies of psi: set 0 = L.sor (the caller's output), set 1 = L.alt
-    double* const s0r = L.sor[0];
-    double* const s0b = L.sor[1];
-    double* const s1r = L.alt[0];
-    double* const s1b = L.alt[1];
-
-    int k = 1, conv_k = -1, status = CNV_NOT_CONVERGED;
-    double e_last = 0.0;
-    const int kmax = p.itmax;  // sweeps 1..itmax correspond to the reference's k = 0..itmax-1
-
-    // Check e_j (1 <= j); returns 0 run on, 1 converged at j, 2 failure.
-    auto check = [&](int j) -> int {
-        if (threadIdx.x == 0) {
-            int res = 0;
-            const int slot = j % kRing;
-            if (!wait_geq(&sy->count[slot], (unsigned)gridDim.x, ctl, p.timeout_ns)) {
-                res = 2;
-            } else {
-                unsigned long long c[4];
+// Signal warp, lane 0: waits until every block has added e_j and evaluates the stop test.
+// Returns 0 run on, 1 e_j < tol, 2 wait given up, 3 non-finite; e_j in *e.
+__device__ int check_norm(SyncState* sy, int j, const PoissonParams& p, Ctrl* ctl, double* e) {
+    const int slot = j % kRing;
+    if (!wait_geq(&sy->count[slot], (unsigned)gridDim.x, ctl, p.timeout_ns)) return 2;
+    unsigned long long c[4];
 #pragma unroll
-                for (int w = 0; w < 4; ++w) c[w] = __ldcg(&sy->acc[slot][w]);
-                // carry-propagate the 32-bit chunks into a 128-bit value
-                unsigned long long t = c[0];
-                unsigned long long lo = t & 0xffffffffull;
-                t = c[1] + (t >> 32);
-                lo |= (t & 0xffffffffull) << 32;
-                t = c[2] + (t >> 32);
-                unsigned long long hi = t & 0xffffffffull;
-                t = c[3] + (t >> 32);
-                hi |= t << 32;
-                const double e = from_fixed96(lo, hi);
-                s_e = e;
-                if (__ldcg(&sy->nonfinite[slot]) || !isfinite(e)) res = 3;
-                else if (e < p.tol) res = 1;
-            }
-            s_stop = res;
-        }
-        __syncthreads();
-        const int r = s_stop;
-        __syncthreads();
-        return r;
-    };
+    for (int w = 0; w < 4; ++w) c[w] = __ldcg(&sy->acc[slot][w]);
+    // carry-propagate the 32-bit chunks into a 128-bit value
+    unsigned long long t = c[0];
+    unsigned long long lo = t & 0xffffffffull;
+    t = c[1] + (t >> 32);
+    lo |= (t & 0xffffffffull) << 32;
+    t = c[2] + (t >> 32);
+    unsigned long long hi = t & 0xffffffffull;
+    t = c[3] + (t >> 32);
+    hi |= t << 32;
+    *e = from_fixed96(lo, hi);
+    if (__ldcg(&sy->nonfinite[slot]) || !isfinite(*e)) return 3;
+    return *e < p.tol ? 1 : 0;
+}
 
-    for (k = 1; k <= kmax; ++k) {
-        if (k >= 3) {
-            const int r = check(k - 2);
-            if (r == 1) { conv_k = k - 2; status = CNV_OK; e_last = s_e; break; }
-            if (r == 2) { status = CNV_TIMEOUT; break; }
-            if (r == 3) { status = CNV_NONFINITE; e_last = s_e; break; }
-            e_last = s_e;
-            if (me == 0 && threadIdx.x == 0 && k >= 5) {
-                // everyone has read e_{k-4} (they all finished sweep k-2); reuse its slot
+// The signal warp's whole run: per sweep one DEC arrival, one NORM wait (the previous sweep's
+// partials) and per half-sweep one GO arrival and one PUB wait; it ends with the verdict in
+// sh.status, sh.conv_k, sh.e_last. Every barrier instance is complete before the next instance
+// of the same barrier can be entered: each next arrival of the signal warp follows a PUB wait
+// that needs the frame warps past the previous instance, and each next arrival of the cell
+// warps follows a GO or END that needs the signal warp past it.
+template <int KIND>
+__device__ void signal_warp(const PoissonParams& p, const Tile& t, SyncState* sy, Ctrl* ctl, Shared& sh) {
+    const int lane = threadIdx.x & 31;
+    const int me = blockIdx.x;
+    const int kmax = p.itmax;
+    constexpr int kHalves = KIND == CNV_POISSON_JACOBI ? 1 : 2;
+    int status = CNV_NOT_CONVERGED, conv_k = -1;
+    double e_last = 0.0;
+    bool gave_up = false;
+    bool stopped = false;
+    for (int k = 1; k <= kmax; ++k) {
+        // verdict before sweep k: e_{k-2} (its shares were added during sweep k-1)
+        int v = gave_up ? 2 : 0;
+        if (lane == 0 && !gave_up && k >= 3) {
+            double e = 0.0;
+            v = check_norm(sy, k - 2, p, ctl, &e);
+            if (v != 2) e_last = e;
+            if (v == 0 && me == 0 && k >= 5) {
+                // everyone has read e_{k-4} (they all added e_{k-2}); reuse its slot
                 const int slot = (k - 4) % kRing;
 #pragma unroll
                 for (int w = 0; w < 4; ++w) sy->acc[slot][w] = 0;
@@ -299,6 +370,87 @@ __global__ void __launch_bounds__(kThreads, 2) k_poisson(PoissonLaunch L) {
                 atomicExch(&sy->count[slot], 0u);
             }
         }
+        v = __shfl_sync(0xffffffffu, v, 0);
+        if (lane == 0) sh.stop[k & 1] = v;
+        __syncwarp();
+        bar_arrive(kBarDec, kThreads);
+        if (v) {
+            if (v == 1) { status = CNV_OK; conv_k = k - 2; }
+            else if (v == 2) status = CNV_TIMEOUT;
+            else status = CNV_NONFINITE;
+            if (k >= 2) bar_sync(kBarNorm, kThreads);  // sweep k-1's partials, left unused
+            stopped = true;
+            break;
+        }
+#pragma unroll
+        for (int h = 0; h < kHalves; ++h) {
+            // red (and Jacobi) needs the neighbours' black frames of sweep k-1; black their red of k
+            const unsigned* fl = h == 0 ? sy->flag[1] : sy->flag[0];
+            const unsigned want = h == 0 ? (unsigned)(k - 1) : (unsigned)k;
+            bool ok = true;
+            if (lane < 4 && !gave_up) {
+                const int nb = t.nb[lane];
+                if (nb >= 0) ok = wait_geq(fl + nb, want, ctl, p.timeout_ns);
+            }
+            if (!__all_sync(0xffffffffu, ok)) gave_up = true;
+            // Sweep k-1's norm partials. Taken before this sweep's first GO: the cell warps
+            // cannot reach sweep k's NORM before every frame warp has passed that GO, so the
+            // two NORM instances never overlap (with one half-sweep per sweep, Jacobi, there
+            // is no later GO to order them).
+            if (h == 0 && k >= 2) bar_sync(kBarNorm, kThreads);
+            bar_arrive(kBarGo, kGoThreads);
+            bar_sync(kBarPub, kGoThreads);
+            if (lane == 0) {
+                __threadfence();
+                st_release(&sy->flag[KIND == CNV_POISSON_JACOBI ? 1 : h][me], (unsigned)k);
+            }
+            __syncwarp();
+            // sh.part[(k-1) & 1] is next written at the end of sweep k+1, after sweep k+1's GO
+            if (h == 0 && k >= 2) {
+                if (lane == 0) contribute(sy, k - 1, sh);
+                __syncwarp();
+            }
+        }
+    }
+    if (!stopped && kmax >= 1) {
+        // the last sweep's share, then the tests of sweeps kmax-1 and kmax (not checked yet)
+        bar_sync(kBarNorm, kThreads);
+        if (gave_up) {
+            status = CNV_TIMEOUT;
+        } else if (lane == 0) {
+            contribute(sy, kmax, sh);
+            for (int j = (kmax >= 2 ? kmax - 1 : 1); j <= kmax; ++j) {
+                double e = 0.0;
+                const int v = check_norm(sy, j, p, ctl, &e);
+                if (v != 2) e_last = e;
+                if (v == 1) { conv_k = j; status = CNV_OK; break; }
+                if (v == 2) { status = CNV_TIMEOUT; break; }
+                if (v == 3) { status = CNV_NONFINITE; break; }
+            }
+        }
+    }
+    if (lane == 0) {
+        sh.status = status;
+        sh.conv_k = conv_k;
+        sh.e_last = e_last;
+    }
+}
+
+// The cell warps' whole run: the mirror image of signal_warp's barrier sequence.
+template <Arith A, int KIND, bool FOLD>
+__device__ void cell_warps(const PoissonLaunch& L, const Tile& t, Shared& sh) {
+    const PoissonParams& p = L.p;
+    const int warp = threadIdx.x >> 5;
+    const bool frame_warp = warp < kFrameWarps;
+    // two copies of psi: set 0 = L.sor (the caller's output), set 1 = L.alt
+    double* const s0r = L.sor[0];
+    double* const s0b = L.sor[1];
+    double* const s1r = L.alt[0];
+    double* const s1b = L.alt[1];
+    int half = 0;
+    for (int k = 1; k <= p.itmax; ++k) {
+        bar_sync(kBarDec, kThreads);
+        if (sh.stop[k & 1]) break;
         // sweep k reads set (k-1)&1 and writes set k&1
         const bool odd = k & 1;
         SweepPtrs q;
@@ -312,73 +464,94 @@ __global__ void __launch_bounds__(kThreads, 2) k_poisson(PoissonLaunch L) {
         if (KIND == CNV_POISSON_JACOBI) {
             q.oth[0] = q.prev[1];
             q.oth[1] = q.prev[0];
-            if (!neighbours_at(sy->flag[1], t, (unsigned)(k - 1), ctl, p.timeout_ns, s_ok)) { status = CNV_TIMEOUT; break; }
-            frame_pass<A, KIND, FOLD, 2>(p, t, q, acc);
-            publish(&sy->flag[1][me], (unsigned)k);
-            if (threadIdx.x == 32 && k > 1) contribute(sy, k - 1, s_chunk, s_big);
-            interior_pass<A, KIND, FOLD, 2>(p, t, q, acc);
-            __syncthreads();
+            if (frame_warp) {
+                bar_sync(kBarGo, kGoThreads);
+                frame_pass<A, KIND, FOLD, 2>(p, t, q, acc);
+                __syncwarp();
+                bar_arrive(kBarPub, kGoThreads);
+            }
+            interior_chunks<A, KIND, FOLD, 2>(p, t, q, acc, &sh.ctr[half & 1]);
+            bar_sync(kBarEnd, kCellThreads);
+            if (threadIdx.x == 0) sh.ctr[half & 1] = 0;
+            ++half;
         } else {
             // red: black neighbours of sweep k-1, own red of sweep k-1
             q.oth[0] = q.prev[1];
             q.oth[1] = q.next[0];  // black: red of sweep k (new), own black of sweep k-1
-            if (!neighbours_at(sy->flag[1], t, (unsigned)(k - 1), ctl, p.timeout_ns, s_ok)) { status = CNV_TIMEOUT; break; }
-            frame_pass<A, KIND, FOLD, 0>(p, t, q, acc);
-            publish(&sy->flag[0][me], (unsigned)k);
-            if (threadIdx.x == 32 && k > 1) contribute(sy, k - 1, s_chunk, s_big);
-            interior_pass<A, KIND, FOLD, 0>(p, t, q, acc);
-            __syncthreads();
-            if (!neighbours_at(sy->flag[0], t, (unsigned)k, ctl, p.timeout_ns, s_ok)) { status = CNV_TIMEOUT; break; }
-            frame_pass<A, KIND, FOLD, 1>(p, t, q, acc);
-            publish(&sy->flag[1][me], (unsigned)k);
-            interior_pass<A, KIND, FOLD, 1>(p, t, q, acc);
-            __syncthreads();
+            if (frame_warp) {
+                bar_sync(kBarGo, kGoThreads);
+                frame_pass<A, KIND, FOLD, 0>(p, t, q, acc);
+                __syncwarp();
+                bar_arrive(kBarPub, kGoThreads);
+            }
+            interior_chunks<A, KIND, FOLD, 0>(p, t, q, acc, &sh.ctr[half & 1]);
+            bar_sync(kBarEnd, kCellThreads);
+            if (threadIdx.x == 0) sh.ctr[half & 1] = 0;
+            ++half;
+            if (frame_warp) {
+                bar_sync(kBarGo, kGoThreads);
+                frame_pass<A, KIND, FOLD, 1>(p, t, q, acc);
+                __syncwarp();
+                bar_arrive(kBarPub, kGoThreads);
+            }
+            interior_chunks<A, KIND, FOLD, 1>(p, t, q, acc, &sh.ctr[half & 1]);
+            bar_sync(kBarEnd, kCellThreads);
+            if (threadIdx.x == 0) sh.ctr[half & 1] = 0;
+            ++half;
         }
-        // this block's share of e_k: integer chunk sums (exact, order-free); thread 32 adds them
-        // to the ring during the next sweep's interior pass, where no barrier waits for its fence
-        {
+        // this warp's share of e_k: integer chunk sums (exact, order-free), handed to the
+        // signal warp, which adds the block's total during the next sweep
 #pragma unroll
-            for (int w = 0; w < 4; ++w) {
-                unsigned long long x = acc.c[w];
+        for (int w = 0; w < 4; ++w) {
+            unsigned long long x = acc.c[w];
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
-                acc.c[w] = x;
-            }
-            const unsigned big = __any_sync(0xffffffffu, acc.big) ? 1u : 0u;
-            if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-                for (int w = 0; w < 4; ++w) s_wchunk[threadIdx.x >> 5][w] = acc.c[w];
-                s_wbig[threadIdx.x >> 5] = big;
-            }
-            __syncthreads();
-            if (threadIdx.x < 4) {
-                unsigned long long x = 0;
-                for (int w = 0; w < kThreads / 32; ++w) x += s_wchunk[w][threadIdx.x];
-                s_chunk[threadIdx.x] = x;
-            } else if (threadIdx.x == 4) {
-                unsigned b2 = 0;
-                for (int w = 0; w < kThreads / 32; ++w) b2 |= s_wbig[w];
-                s_big = b2;
-            }
-            __syncthreads();
+            for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+            acc.c[w] = x;
         }
+        const unsigned big = __any_sync(0xffffffffu, acc.big) ? 1u : 0u;
+        if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+            for (int w = 0; w < 4; ++w) sh.part[k & 1][warp][w] = acc.c[w];
+            sh.pbig[k & 1][warp] = big;
+        }
+        __syncwarp();
+        bar_arrive(kBarNorm, kThreads);
     }
-    // the last sweep's share is still pending when the loop runs out of sweeps
-    if (status == CNV_NOT_CONVERGED && k > kmax && threadIdx.x == 32) contribute(sy, kmax, s_chunk, s_big);
-    if (status == CNV_NOT_CONVERGED && k > kmax) {
-        // sweeps kmax-1 and kmax are not checked yet
-        for (int j = (kmax >= 2 ? kmax - 1 : 1); j <= kmax; ++j) {
-            const int r = check(j);
-            if (r == 1) { conv_k = j; status = CNV_OK; e_last = s_e; break; }
-            if (r == 2) { status = CNV_TIMEOUT; break; }
-            if (r == 3) { status = CNV_NONFINITE; e_last = s_e; break; }
-            e_last = s_e;
-        }
+}
+
+template <Arith A, int KIND, bool FOLD>
+__global__ void __launch_bounds__(kThreads, 2) k_poisson(PoissonLaunch L) {
+    Ctrl* ctl = L.ctrl;
+    const PoissonParams& p = L.p;
+    SyncState* sy = reinterpret_cast<SyncState*>(L.sync);
+    const Geometry geo{p.n, p.pitch, L.gx, L.gy};
+    const Tile t = make_tile(geo, blockIdx.x);
+    __shared__ Shared sh;
+    __shared__ int s_abort;
+    if (threadIdx.x < 2) {
+        sh.ctr[threadIdx.x] = 0;
+        sh.stop[threadIdx.x] = 0;
     }
+    if (threadIdx.x == 0) s_abort = ld_volatile_int(&ctl->abort);
+    __syncthreads();
+    if (s_abort) return;  // one read for the whole block: the warp roles must all run or none
+
+    if ((threadIdx.x >> 5) == kSignalWarp)
+        signal_warp<KIND>(p, t, sy, ctl, sh);
+    else
+        cell_warps<A, KIND, FOLD>(L, t, sh);
+    __syncthreads();
+
+    const int status = sh.status;
+    const int conv_k = sh.conv_k;
     if (status == CNV_TIMEOUT) return;
     // the answer is the iterate of sweep conv_k (or of the last sweep): copy it into set 0
-    const int ans = conv_k > 0 ? conv_k : kmax;
+    const int ans = conv_k > 0 ? conv_k : p.itmax;
     if (ans & 1) {
+        double* const s0r = L.sor[0];
+        double* const s0b = L.sor[1];
+        const double* const s1r = L.alt[0];
+        const double* const s1b = L.alt[1];
         const int h = t.r1 - t.r0, w = t.c1 - t.c0;
         for (int x = threadIdx.x; x < h * w; x += kThreads) {
             const int i = t.r0 + x / w, j = t.c0 + x % w;
@@ -387,7 +560,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_poisson(PoissonLaunch L) {
             else s0r[idx] = s1r[idx];
         }
     }
-    if (me == 0 && threadIdx.x == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const double e_last = sh.e_last;
         const int iters = status == CNV_OK ? conv_k - 1 : p.itmax;
         ctl->iters = iters;
         ctl->err = e_last;

@@ -131,9 +131,10 @@ __device__ __forceinline__ bool big_or_zero(double x) {
     return ((hi & 0x7ff00000) >= (63 << 20)) || (((hi & 0x7fffffff) | lo) == 0);
 }
 
+// The new value of one cell (no norm).
 template <Arith A, int KIND, bool FOLD>
-__device__ __forceinline__ double point_update(const PoissonParams& p, double up, double dn, double rt,
-                                               double lt, double g, double old, NormAcc& acc) {
+__device__ __forceinline__ double point_value(const PoissonParams& p, double up, double dn, double rt,
+                                              double lt, double g, double old) {
     double nw;
     if (A == Arith::kExact) {
         if (FOLD) {
@@ -167,14 +168,21 @@ __device__ __forceinline__ double point_update(const PoissonParams& p, double up
                 nw = p.den_pow2 ? __dmul_rn(num, p.rden) : __ddiv_rn(num, p.den);
             }
         }
-        norm_add(acc, nw, old);
         return nw;
     } else {
         const double gs = fma(p.wy, up + dn, fma(p.wx, rt + lt, -g));
         nw = KIND == CNV_POISSON_SOR ? fma(p.beta, gs - old, old) : gs;
-        norm_add(acc, nw, old);
         return nw;
     }
+}
+
+// The new value of one cell, with |new - old| added to the stop norm.
+template <Arith A, int KIND, bool FOLD>
+__device__ __forceinline__ double point_update(const PoissonParams& p, double up, double dn, double rt,
+                                               double lt, double g, double old, NormAcc& acc) {
+    const double nw = point_value<A, KIND, FOLD>(p, up, dn, rt, lt, g, old);
+    norm_add(acc, nw, old);
+    return nw;
 }
 
 }  // namespace
