@@ -79,6 +79,7 @@ _SIGS = {
     "cnv_poisson": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int), _dp]),
     "cnv_poisson_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), _dp]),
     "cnv_last_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _dp, _dp]),
+    "cnv_solver_info": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "cnv_poisson_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
                                       C.c_int, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), _dp,
                                       C.c_void_p]),
@@ -237,6 +238,12 @@ class Cavity:
         it, err = C.c_int(0), C.c_double(0.0)
         rc = self._lib.cnv_poisson(self._h, _ptr(np.ascontiguousarray(f)), _ptr(psi), C.byref(it), C.byref(err))
         return rc, psi, it.value, err.value
+
+    def solver_info(self) -> str:
+        """The Poisson solver this cavity runs and its geometry (cnv_solver_info)."""
+        buf = C.create_string_buffer(256)
+        check(self._lib.cnv_solver_info(self._h, buf, 256), "cnv_solver_info")
+        return buf.value.decode()
 
     def stats(self):
         """(sweeps, ms of the last call, ms of the last Poisson kernel) -- CUDA-event times."""

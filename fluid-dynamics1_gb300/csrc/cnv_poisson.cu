@@ -628,14 +628,29 @@ void poisson_tiles(int n, int grid, int* gx, int* gy) {
 }
 
 int poisson_grid_for(int n, int sms, int per_sm) {
-    // one block (512 threads) per about 2048 interior cells, at most 2 per SM, and a multiple
-    // of the SM count once the grid covers the GPU so that every SM gets the same work
+    // Two blocks per SM from about 3000 interior cells per block: the second block's warps hide
+    // FP64 latency (1024^2: 18.0 us per sweep on 2 x 152 blocks, 18.8 on 152); one per SM from
+    // about 700 cells per block (768^2: 26.0 us on 152 blocks, 26.9 on 304); below that one
+    // block per about 700 cells, picking among the nearby counts the one whose tiles have the
+    // smallest frames (a prime count would only tile as strips).
     const long long cells = (long long)(n - 2) * (n - 2);
     const int cap = std::min(std::min(per_sm, 2) * sms, kMaxSolverBlocks);
-    long long want = cells / 2048;
-    if (want >= 2LL * sms && cap >= 2 * sms) return 2 * sms;
-    if (want >= sms) return std::min(sms, cap);
-    return (int)std::max(1LL, std::min<long long>(want, cap));
+    if (cells >= 2LL * sms * 3000 && cap >= 2 * sms) return 2 * sms;
+    if (cells >= 700LL * sms) return std::min(sms, cap);
+    const int want = (int)std::max(1LL, std::min<long long>(cells / 700, cap));
+    const double ni = n - 2;
+    int best = want;
+    double best_score = 1e300;
+    for (int g = std::max(1, want - want / 4); g <= want; ++g) {
+        int gx = 1, gy = 1;
+        poisson_tiles(n, g, &gx, &gy);
+        const double score = (double)cells / g + 3.0 * (ni / gx + ni / gy);  // cells + frame per block
+        if (score < best_score) {
+            best_score = score;
+            best = g;
+        }
+    }
+    return best;
 }
 
 cudaError_t launch_poisson(const PoissonLaunch& L, cudaStream_t s) {

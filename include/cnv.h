@@ -263,6 +263,12 @@ int cnv_adjoint_stats(cnv_adjoint *a, double *forward_ms, double *backward_ms, l
  * the last step or solve it ran (ms). Any pointer may be NULL. */
 int cnv_last_stats(cnv_state *s, long long *sweeps, double *ms, double *poisson_ms);
 
+/* One line naming the Poisson solver this state runs and its geometry, e.g.
+ * "sor-exchange grid=304 tiles=16x19" (FP64 SOR/GS exchanging every half-sweep),
+ * "sor-tiled sweeps=4 grid=150 tiles=5x30", "mixed grid=152 tiles=8x19" or
+ * "direct-sine-transform". Returns CNV_BAD_ARG if it does not fit in len bytes. */
+int cnv_solver_info(cnv_state *s, char *buf, size_t len);
+
 /* ---------------------------------------------------------------------------------------
  * Pieces of the step for callers that keep the reference's loop: the Euler update of
  * src/fluiddyn.c:71-102 from caller-supplied derivative fields (count points, in place on w,

@@ -140,10 +140,12 @@ def test_poisson_alone_matches_oracle(cnv, orc, ptype, n, blocking):
     cfg = make_cfg(cnv, n, poisson_type=ptype, poisson_tol=1e-9, poisson_max_it=200000, sor_blocking=blocking)
     with cnv.Cavity(cfg) as cav:
         rc, psi, it, err = cav.poisson(f)
+        sweeps, ms, poisson_ms = cav.stats()  # the standalone solve's sweeps and kernel time
     p = oracle_params(orc, cfg)
     opsi, oit, oerr, orc_rc = orc.poisson(p, f)
     assert rc == 0 and orc_rc == 0
     assert it == oit
+    assert sweeps == it + 1 and poisson_ms > 0
     assert bitwise(psi, opsi)
     assert abs(err - oerr) <= REL_ERR_TOL * oerr
 
