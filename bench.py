@@ -275,7 +275,8 @@ def run_device(cnvpy, w, device, steps, warmup, flush, precision=0, poisson_type
             rc, info = cav.step(1)
             sweeps, ms, pms = cav.stats()
             if t >= warmup:
-                recs.append(dict(ms=ms, poisson_ms=pms, sweeps=sweeps, iters=info[0]["iters"]))
+                recs.append(dict(ms=ms, poisson_ms=pms, sweeps=sweeps, iters=info[0]["iters"],
+                                 solver=cav.solver_info()))
         out = cav.get_fields() if fields else None
     return (recs, out) if fields else recs
 
@@ -510,7 +511,7 @@ def ours(args):
         "config": {"workload": workload_name(w), "grid": w["n"], "precision": prec_name,
                    "l2": "flushed before every timed step (256 MB device write)" if flush.active else "not flushed",
                    "parallelism": f"replicas x{ws}", "sweeps_per_step": round(sweeps / len(recs), 1),
-                   "first_step": args.warmup},
+                   "first_step": args.warmup, "solver": recs[0]["solver"] if recs else None},
         "Mcell_sweeps_per_s": round(interior * sweeps / (pms * 1e-3) / 1e6, 2),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
