@@ -8,7 +8,7 @@ Tolerances: the FP64 path with reference arithmetic (precision = fp64) must matc
 bit for bit on every field (same operation order, round-to-nearest, no FMA contraction);
 iteration counts must be equal; the stop norm is summed in a different order on the GPU, so it
 is compared to 1e-12 relative. The FMA form must agree to 1e-10 normwise relative
-(max|a-b| / max|b|) per field, inside the benchmark spec's bound of 1e-8 relative.
+(max|a-b| / max|b|) per field, well inside the 1e-8 relative bound the FMA form is held to.
 """
 from __future__ import annotations
 
