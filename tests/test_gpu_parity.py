@@ -210,6 +210,23 @@ def test_blocking_flag_checks(cnv):
         assert e.value.status == cnv.CNV_BAD_ARG
 
 
+@pytest.mark.parametrize("n,kw,want", [
+    (256, {}, "sor-tiled sweeps=4"),                       # the tiled kernel below 300^2
+    (320, {}, "sor-exchange"),                             # the exchange kernel from 300^2
+    (512, {}, "sor-exchange grid=152 tiles=8x19"),         # one block per SM (not 127 strips)
+    (1024, {}, "sor-exchange grid=304 tiles=16x19"),       # two blocks per SM
+    (1024, {"precision": 2}, "mixed grid=152"),
+    (256, {"poisson_type": 4}, "direct-sine-transform"),
+    (256, {"sor_blocking": 1}, "sor-exchange"),
+])
+def test_solver_choice_and_geometry(cnv, n, kw, want):
+    """cnv_solver_info names the solver a state picked; the defaults follow the measured
+    crossovers (tiled kernel below 300^2, one block per SM up to about 6000 cells per SM)."""
+    with cnv.Cavity(make_cfg(cnv, n, **kw)) as cav:
+        info = cav.solver_info()
+    assert info.startswith(want), info
+
+
 def test_nonfinite_input_rejected(cnv):
     cfg = make_cfg(cnv, 16)
     with cnv.Cavity(cfg) as cav:
