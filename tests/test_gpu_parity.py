@@ -132,6 +132,19 @@ def test_config1_64_re100_sor15(cnv, orc):
     assert [s["iters"] for s in gs] == [s["iters"] for s in os_]
 
 
+def test_config1_all_1000_steps(cnv, orc):
+    """The whole CPU workload (64^2, Re 100, dt 1e-3, SOR beta 1.5, tol 1e-6, tf = 1 -> 1000
+    steps, about 1.7 M SOR sweeps): every step's iteration count equal to the oracle's and the
+    fields after the last step equal bit for bit."""
+    steps = 1000
+    cfg = make_cfg(cnv, 64, Re=100.0, dt=1e-3, poisson_tol=1e-6, sor_omega=1.5)
+    g, gs, o, os_ = run_both(cnv, orc, cfg, steps)
+    assert len(gs) == len(os_) == steps
+    assert [s["iters"] for s in gs] == [s["iters"] for s in os_]
+    for name, a, b in zip("w u v psi".split(), g, o):
+        assert bitwise(a, b), f"{name} differs: max abs {np.max(np.abs(a - b))}"
+
+
 @pytest.mark.parametrize("ptype,blocking", [(1, 1), (2, 1), (3, 1), (1, 2), (2, 2), (1, 4), (2, 4)])
 @pytest.mark.parametrize("n", [16, 37, 96])
 def test_poisson_alone_matches_oracle(cnv, orc, ptype, n, blocking):
