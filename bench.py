@@ -13,7 +13,9 @@ before every timed step. e2e = the same metric through the C ABI with host buffe
 uploads w, u, v from pinned host memory, runs, and reads w, u, v, psi back, all inside the
 timed region. roofline = the persistent Poisson kernel, algorithmic bytes (24 B per interior
 cell per sweep: read psi and f, write psi) over its CUDA-event duration, against the measured
-HBM copy bandwidth. cpu_baseline = the CPU oracle (a restatement of the reference's own
+HBM copy bandwidth; roofline.fp64_pipe = the same kernel's FP64 rate (7 add/multiply operations
+per cell-sweep), against the device's rate for that mix measured by a probe kernel in the same
+run -- the ceiling that binds, since the solve runs from L2. cpu_baseline = the CPU oracle (a restatement of the reference's own
 algorithm) on this host's cores for one step of the same workload.
 
 forms = the other ways the library takes the step, each timed the same way and compared field by
@@ -474,6 +476,15 @@ def ours(args):
     achieved = alg_bytes / (pms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = profiled_traffic_per_launch() if args.form == "fp64" else None
+    fp64 = None
+    if args.form == "fp64":
+        # the binding ceiling: 7 FP64 add/multiply operations per interior cell-sweep, against
+        # the device's own rate for that instruction mix (probe kernels, same process)
+        add_mul, fma_rate = cnvpy.probe_fp64(local)
+        ops = 7.0 * interior * sweeps / (pms * 1e-3)
+        fp64 = {"achieved_gops": round(ops / 1e9, 1), "peak_gops": round(add_mul / 1e9, 1),
+                "frac": round(ops / add_mul, 4), "fma_peak_gops": round(fma_rate / 1e9, 1),
+                "peak_source": "probe kernel: independent round-to-nearest multiply-then-add chains"}
 
     e2e_s, pinned = run_e2e(cnvpy, w, local, args.steps, args.warmup)
     e2e_s = dist.max(e2e_s)
@@ -515,7 +526,7 @@ def ours(args):
         "Mcell_sweeps_per_s": round(interior * sweeps / (pms * 1e-3) / 1e6, 2),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                     "kernel": kernel},
+                     "kernel": kernel, "fp64_pipe": fp64},
         "e2e": e2e,
         "gpu_launches": 5 * args.steps,
         "clocks": clk,

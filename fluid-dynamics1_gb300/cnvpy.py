@@ -80,6 +80,7 @@ _SIGS = {
     "cnv_poisson_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), _dp]),
     "cnv_last_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _dp, _dp]),
     "cnv_solver_info": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    "cnv_probe_fp64": (C.c_int, [C.c_int, _dp, _dp]),
     "cnv_poisson_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
                                       C.c_int, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), _dp,
                                       C.c_void_p]),
@@ -331,6 +332,13 @@ class Batch:
         cells, sweeps, ms = C.c_longlong(0), C.c_longlong(0), C.c_double(0)
         check(self._lib.cnv_batch_stats(self._h, C.byref(cells), C.byref(sweeps), C.byref(ms)), "cnv_batch_stats")
         return cells.value, sweeps.value, ms.value
+
+
+def probe_fp64(device: int = 0):
+    """(multiply-then-add chains, FMA chains): FP64 lane-operations per second of the device."""
+    a, f = C.c_double(0), C.c_double(0)
+    check(load().cnv_probe_fp64(device, C.byref(a), C.byref(f)), "cnv_probe_fp64")
+    return a.value, f.value
 
 
 def noise_field(n: int, seed: int, sigma: float = 1.0, passes: int = 0):

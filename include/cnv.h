@@ -299,6 +299,12 @@ int cnv_write_vtk(const char *output_dir, const char *title, int count, const do
  * splitmix64 stream seeded with seed, then `passes` Jacobi averaging passes over the interior. */
 int cnv_noise_field(int n, unsigned long long seed, double sigma, int passes, double *out);
 
+/* FP64 arithmetic throughput of a device, measured in place: lane-operations per second of
+ * independent round-to-nearest multiply-then-add chains (the exact Poisson update's instruction
+ * mix) and of fused multiply-adds (each FMA one operation). Either pointer may be NULL (not
+ * both). Runs about 0.3 s of probe kernels on the device's default stream. */
+int cnv_probe_fp64(int device, double *add_mul_ops_per_s, double *fma_ops_per_s);
+
 /* Human-readable text for the last failing call on this thread. */
 const char *cnv_last_error(void);
 /* Library version and the device it was built for. */

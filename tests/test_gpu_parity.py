@@ -349,3 +349,12 @@ def test_mixed_warm_start_needs_fewer_corrections(cnv):
         assert rc == 0
         counts[warm] = sum(s["iters"] for s in steps[1:])
     assert counts[1] < counts[0], counts
+
+
+def test_fp64_probe_reports_device_rates(cnv):
+    """cnv_probe_fp64: positive rates of the right order for a GB300-class part (FP64 is
+    about 1/60 of FP32 there: 1e11-1e13 operations per second), FMA chains not slower than
+    multiply-then-add chains by more than rounding of the timing."""
+    add_mul, fma_rate = cnv.probe_fp64(0)
+    assert 1e11 < add_mul < 1e13 and 1e11 < fma_rate < 1e13
+    assert fma_rate > 0.5 * add_mul
