@@ -478,12 +478,14 @@ def ours(args):
     traffic = profiled_traffic_per_launch() if args.form == "fp64" else None
     fp64 = None
     if args.form == "fp64":
-        # the binding ceiling: 7 FP64 add/multiply operations per interior cell-sweep, against
-        # the device's own rate for that instruction mix (probe kernels, same process)
+        # the binding ceiling: the update's 7 FP64 add/multiply operations per interior cell-sweep
+        # (5 on the FP64 pipe, the 2 multiplications by constants in exact integer arithmetic),
+        # against the device's own FP64 rate for that mix (probe kernels, same process)
         add_mul, fma_rate = cnvpy.probe_fp64(local)
         ops = 7.0 * interior * sweeps / (pms * 1e-3)
         fp64 = {"achieved_gops": round(ops / 1e9, 1), "peak_gops": round(add_mul / 1e9, 1),
                 "frac": round(ops / add_mul, 4), "fma_peak_gops": round(fma_rate / 1e9, 1),
+                "ops_per_cell_sweep": 7, "on_fp64_pipe_per_cell_sweep": 5,
                 "peak_source": "probe kernel: independent round-to-nearest multiply-then-add chains"}
 
     e2e_s, pinned = run_e2e(cnvpy, w, local, args.steps, args.warmup)

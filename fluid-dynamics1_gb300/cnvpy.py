@@ -81,6 +81,7 @@ _SIGS = {
     "cnv_last_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _dp, _dp]),
     "cnv_solver_info": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "cnv_probe_fp64": (C.c_int, [C.c_int, _dp, _dp]),
+    "cnv_check_mul_rn": (C.c_int, [C.c_int, _dp, C.c_int, C.c_double, _dp]),
     "cnv_poisson_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
                                       C.c_int, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), _dp,
                                       C.c_void_p]),
@@ -339,6 +340,14 @@ def probe_fp64(device: int = 0):
     a, f = C.c_double(0), C.c_double(0)
     check(load().cnv_probe_fp64(device, C.byref(a), C.byref(f)), "cnv_probe_fp64")
     return a.value, f.value
+
+
+def check_mul_rn(x, c: float, device: int = 0):
+    """c * x on the device the way the exact update multiplies by its constants."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    check(load().cnv_check_mul_rn(device, _ptr(x), x.size, c, _ptr(out)), "cnv_check_mul_rn")
+    return out
 
 
 def noise_field(n: int, seed: int, sigma: float = 1.0, passes: int = 0):

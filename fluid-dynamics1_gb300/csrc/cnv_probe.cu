@@ -8,6 +8,7 @@
 #include <cstdio>
 
 #include "cnv_internal.h"
+#include "cnv_sor.cuh"
 
 namespace cnv {
 namespace {
@@ -57,6 +58,41 @@ int time_probe(int sms, double* out, double* ops_per_s) {
 
 }  // namespace
 }  // namespace cnv
+
+namespace cnv {
+namespace {
+
+__global__ void k_mul_rn(const double* x, int count, double c, double* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) out[i] = mul_rn(c, x[i]);
+}
+
+}  // namespace
+}  // namespace cnv
+
+extern "C" int cnv_check_mul_rn(int device, const double* x, int count, double c, double* out) {
+    using namespace cnv;
+    if (!x || !out || count < 0) {
+        set_last_error("cnv_check_mul_rn: bad argument");
+        return CNV_BAD_ARG;
+    }
+    if (count == 0) return CNV_OK;
+    double* d = nullptr;
+    const size_t bytes = (size_t)count * sizeof(double);
+    int rc = CNV_OK;
+    if (cudaSetDevice(device) != cudaSuccess || cudaMalloc(&d, 2 * bytes) != cudaSuccess) {
+        set_last_error("cnv_check_mul_rn: device setup failed");
+        return CNV_CUDA_ERROR;
+    }
+    if (cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice) != cudaSuccess) rc = CNV_CUDA_ERROR;
+    if (rc == CNV_OK) {
+        k_mul_rn<<<(count + 255) / 256 < 4096 ? (count + 255) / 256 : 4096, 256>>>(d, count, c, d + count);
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, d + count, bytes, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = CNV_CUDA_ERROR;
+    }
+    cudaFree(d);
+    if (rc != CNV_OK) set_last_error("cnv_check_mul_rn: kernel or copy failed");
+    return rc;
+}
 
 extern "C" int cnv_probe_fp64(int device, double* add_mul_ops_per_s, double* fma_ops_per_s) {
     using namespace cnv;

@@ -101,6 +101,35 @@ __device__ __forceinline__ void abs_fixed80(double x, unsigned long long& lo, un
 
 // acc += |nw - old|, exactly in fixed point (both truncated at 2^-80), on the integer pipes.
 __device__ __forceinline__ void norm_add(NormAcc& acc, double nw, double old) {
+    {
+        // the common case, same sign and exponent e with 2^-28 <= |x| < 2^46: both images are
+        // exact (no truncation), and their difference is the significands' difference (the
+        // difference of the bit patterns) times 2^(e - 995)
+        const unsigned long long a = (unsigned long long)__double_as_longlong(nw);
+        const unsigned long long b = (unsigned long long)__double_as_longlong(old);
+        const int e = (int)((a >> 52) & 0x7ff);
+        if (((a ^ b) >> 52) == 0 && e >= 995 && e < 1069) {
+            const long long sd = (long long)(a - b);
+            const unsigned long long d = (unsigned long long)(sd < 0 ? -sd : sd);  // < 2^52
+            const int s = e - 995;                                                   // 0 .. 73
+            unsigned long long dl, dh;
+            if (s == 0) {
+                dl = d;
+                dh = 0;
+            } else if (s < 64) {
+                dl = d << s;
+                dh = d >> (64 - s);
+            } else {
+                dl = 0;
+                dh = d << (s - 64);
+            }
+            acc.c[0] += dl & 0xffffffffull;
+            acc.c[1] += dl >> 32;
+            acc.c[2] += dh & 0xffffffffull;
+            acc.c[3] += dh >> 32;
+            return;
+        }
+    }
     unsigned long long al, ah, bl, bh;
     abs_fixed80(nw, al, ah, acc.big);
     abs_fixed80(old, bl, bh, acc.big);
@@ -131,6 +160,61 @@ __device__ __forceinline__ bool big_or_zero(double x) {
     return ((hi & 0x7ff00000) >= (63 << 20)) || (((hi & 0x7fffffff) | lo) == 0);
 }
 
+// x * c rounded to nearest, ties to even, by integer arithmetic, for a normal constant c (bit
+// pattern cb): the 106-bit product of the two 53-bit significands, its top 53 bits, and the
+// IEEE 754 round-half-to-even rule on the rest. A zero x gives the signed zero. Returns false
+// (the caller multiplies on the FP64 pipe instead) for a subnormal, infinite or NaN x, a c that
+// is not normal, and products outside the normal range, so every result equals __dmul_rn(x, c).
+// The exact update uses it for its two multiplications by constants, which moves them from the
+// FP64 pipe (the solver's bottleneck at 7 FP64 operations per cell) to the integer pipes.
+__device__ __forceinline__ bool mul_rn_int(double x, unsigned long long cb, double& out) {
+    const unsigned long long xb = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long sign = (xb ^ cb) & 0x8000000000000000ull;
+    const int ex = (int)((xb >> 52) & 0x7ff);
+    const int ec = (int)((cb >> 52) & 0x7ff);
+    if (ec == 0 || ec == 0x7ff) return false;
+    if (ex == 0) {
+        if ((xb << 1) != 0) return false;  // subnormal
+        out = __longlong_as_double((long long)sign);
+        return true;
+    }
+    if (ex == 0x7ff) return false;
+    const unsigned long long frac = (1ull << 52) - 1;
+    const unsigned long long mx = (xb & frac) | (1ull << 52);
+    const unsigned long long mc = (cb & frac) | (1ull << 52);
+    const unsigned long long lo = mx * mc;
+    const unsigned long long hi = __umul64hi(mx, mc);  // 2^104 <= hi:lo < 2^106
+    const int top = (int)(hi >> 41);                     // 1 when the product is >= 2^105
+    int e = ex + ec - 1023 + top;                        // biased exponent before rounding
+    if (e <= 0) return false;
+    unsigned long long mant, rem, half;
+    if (top) {
+        mant = (hi << 11) | (lo >> 53);
+        rem = lo & ((1ull << 53) - 1);
+        half = 1ull << 52;
+    } else {
+        mant = (hi << 12) | (lo >> 52);
+        rem = lo & ((1ull << 52) - 1);
+        half = 1ull << 51;
+    }
+    mant += (rem > half || (rem == half && (mant & 1))) ? 1 : 0;
+    if (mant >> 53) {  // rounded up to 2^53
+        mant >>= 1;
+        ++e;
+    }
+    if (e >= 0x7ff) return false;
+    out = __longlong_as_double((long long)(sign | ((unsigned long long)e << 52) | (mant & frac)));
+    return true;
+}
+
+// c * x as the exact update computes it: on the integer pipes where mul_rn_int applies, on the
+// FP64 pipe otherwise (the same bits either way).
+__device__ __forceinline__ double mul_rn(double c, double x) {
+    double r;
+    if (!mul_rn_int(x, (unsigned long long)__double_as_longlong(c), r)) r = __dmul_rn(c, x);
+    return r;
+}
+
 // The new value of one cell (no norm).
 template <Arith A, int KIND, bool FOLD>
 __device__ __forceinline__ double point_value(const PoissonParams& p, double up, double dn, double rt,
@@ -145,7 +229,7 @@ __device__ __forceinline__ double point_value(const PoissonParams& p, double up,
             const double t = __dsub_rn(S, g);
             if (big_or_zero(s1) && big_or_zero(s2) && big_or_zero(S) && big_or_zero(t)) {
                 if (KIND == CNV_POISSON_SOR)
-                    nw = __dadd_rn(__dmul_rn(p.b4, t), __dmul_rn(p.omb, old));
+                    nw = __dadd_rn(mul_rn(p.b4, t), mul_rn(p.omb, old));
                 else
                     nw = __dmul_rn(0.25, t);
             } else {

@@ -304,6 +304,10 @@ int cnv_noise_field(int n, unsigned long long seed, double sigma, int passes, do
  * mix) and of fused multiply-adds (each FMA one operation). Either pointer may be NULL (not
  * both). Runs about 0.3 s of probe kernels on the device's default stream. */
 int cnv_probe_fp64(int device, double *add_mul_ops_per_s, double *fma_ops_per_s);
+/* out[i] = c * x[i] computed on the device exactly as the exact Poisson update multiplies by its
+ * constants (integer arithmetic where it applies, the FP64 pipe otherwise): every result must
+ * equal the correctly rounded IEEE product. Host arrays of count doubles. */
+int cnv_check_mul_rn(int device, const double *x, int count, double c, double *out);
 
 /* Human-readable text for the last failing call on this thread. */
 const char *cnv_last_error(void);
