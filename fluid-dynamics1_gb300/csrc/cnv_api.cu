@@ -187,6 +187,7 @@ int validate(const cnv_config* c) {
         return fail(CNV_BAD_ARG, "grid size %d outside [%d, 16384]", c->nx, c->order == 6 ? 5 : 4);
     if (c->poisson_type < 1 || c->poisson_type > 4)
         return fail(CNV_BAD_ARG, "Error - invalid option for Poisson solver (%d)", c->poisson_type);
+    if (c->test_stall_block < 0) return fail(CNV_BAD_ARG, "test_stall_block must be >= 0");
     if (c->sor_blocking != 0 && c->sor_blocking != 1 && c->sor_blocking != 2 && c->sor_blocking != 4)
         return fail(CNV_BAD_ARG, "sor_blocking must be 0 (auto), 1, 2 or 4 sweeps per exchange, got %d",
                     c->sor_blocking);
@@ -618,7 +619,8 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     p.wx = p.dx2 / p.den;
     p.wy = p.dy2 / p.den;
     p.b4 = p.beta / 4;
-    p.timeout_ns = 2000000000LL;  // 2 s per wait for another block
+    p.timeout_ns = (cfg->solver_timeout_ms > 0 ? cfg->solver_timeout_ms : 2000) * 1000000LL;  // per wait
+    p.stall_block = cfg->test_stall_block - 1;
 
     StepArgs& a = s->sa;
     a.n = n;

@@ -118,6 +118,7 @@ extern "C" int cnv_config_set(cnv_config* c, const char* key, const char* v) {
     else if (!strcmp(key, "mixed_max_outer")) c->mixed_max_outer = atoi(v);
     else if (!strcmp(key, "sor_blocking")) c->sor_blocking = atoi(v);
     else if (!strcmp(key, "mixed_warm_start")) c->mixed_warm_start = atoi(v);
+    else if (!strcmp(key, "solver_timeout_ms")) c->solver_timeout_ms = atoi(v);
     else return CNV_BAD_ARG;
     return CNV_OK;
 }

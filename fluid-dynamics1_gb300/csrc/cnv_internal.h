@@ -89,6 +89,7 @@ struct PoissonParams {
     double b4;          // beta / 4 (exact), folded exact form
     int fold;           // 1: exact form with power-of-two scalings folded (dx = dy, dx^2 and den powers of 2)
     long long timeout_ns;  // bound on every wait for another block
+    int stall_block;       // testing only: block of the exchange kernel that never raises its flags (-1: none)
 };
 
 // Set the text cnv_last_error() returns on this thread.

@@ -127,6 +127,7 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
     p.wy = p.dy2 / p.den;
     p.b4 = p.beta / 4;
     p.timeout_ns = 2000000000LL;
+    p.stall_block = -1;
 
     StepArgs a{};
     a.n = n;

@@ -400,7 +400,7 @@ __device__ void signal_warp(const PoissonParams& p, const Tile& t, SyncState* sy
             if (h == 0 && k >= 2) bar_sync(kBarNorm, kThreads);
             bar_arrive(kBarGo, kGoThreads);
             bar_sync(kBarPub, kGoThreads);
-            if (lane == 0) {
+            if (lane == 0 && me != p.stall_block) {  // a stalled block (tests only) never publishes
                 __threadfence();
                 st_release(&sy->flag[KIND == CNV_POISSON_JACOBI ? 1 : h][me], (unsigned)k);
             }

@@ -102,7 +102,11 @@ typedef struct cnv_config {
                                 (the same bits either way) */
     int mixed_warm_start;    /* CNV_PREC_MIXED (and batches): start each step's solve from the previous
                                 step's psi instead of zero (same stop rule: FP64 relative residual) */
-    int reserved[3];
+    int solver_timeout_ms;   /* bound on every on-device wait for another block; <= 0: 2000 */
+    int test_stall_block;    /* testing only: 1 + the index of a block of the FP64 SOR/GS exchange
+                                kernel that never raises its progress flags, so that its neighbours'
+                                bounded waits run out (the solve returns CNV_TIMEOUT); 0: off */
+    int reserved[1];
 } cnv_config;
 
 /* Per-step record: the values the reference logs (src/poisson.c:275, src/main.c:407-408). */

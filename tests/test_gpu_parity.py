@@ -188,7 +188,47 @@ def test_1024_single_step_matches_oracle(cnv, orc, blocking):
     assert gs[0]["iters"] == os_[0]["iters"]
 
 
+def test_1024_four_steps_match_oracle(cnv, orc):
+    """The benchmark workload with its default solver, 4 steps (about 9,600 SOR sweeps): fields bit
+    for bit and every step's iteration count, against the oracle run on all host cores with its
+    exact (order-free) stop norm, the same sum the GPU forms."""
+    n = 1024
+    h = 1.0 / n
+    dt = 0.2 * min(h * h * 1000.0 / 4, h / 1.0)
+    cfg = make_cfg(cnv, n, Re=1000.0, dt=dt, poisson_tol=1e-6, poisson_max_it=100000)
+    with cnv.Cavity(cfg) as cav:
+        rc, gsteps = cav.step(4)
+        g = cav.get_fields()
+    assert rc == 0
+    p = orc.make_params(n, order=cfg.order, re=cfg.Re, dt=cfg.dt, tol=cfg.poisson_tol, itmax=cfg.poisson_max_it,
+                        threads=os.cpu_count() or 1, exact_norm=1)
+    w, u, v, psi = orc.initial_state(n)
+    orc_rc, osteps = orc.run(p, 4, w, u, v, psi)
+    assert orc_rc == 0
+    assert [s["iters"] for s in gsteps] == [s["iters"] for s in osteps]
+    for name, a, b in zip("w u v psi".split(), g, (w, u, v, psi)):
+        assert bitwise(a, b), name
+
+
 # ------------------------------------------------------------------------- failure paths
+@pytest.mark.parametrize("kind", [2, 3], ids=["sor", "jacobi"])
+def test_stalled_block_times_out_and_device_stays_usable(cnv, kind):
+    """A solver block that never raises its progress flags (the test hook test_stall_block):
+    its neighbours' bounded waits run out after solver_timeout_ms, every block leaves through the
+    same barrier sequence, the step reports CNV_TIMEOUT, and the device runs the next solve."""
+    import time
+
+    cfg = make_cfg(cnv, 256, poisson_type=kind, sor_blocking=1, solver_blocks=16, poisson_tol=1e-12,
+                   poisson_max_it=200000, solver_timeout_ms=50, test_stall_block=1 + 5)
+    with cnv.Cavity(cfg) as cav:
+        t0 = time.perf_counter()
+        rc, steps = cav.step(1, raise_on_error=False)
+        elapsed = time.perf_counter() - t0
+    assert rc == cnv.CNV_TIMEOUT, rc
+    assert elapsed < 30, elapsed
+    with cnv.Cavity(make_cfg(cnv, 64, poisson_type=kind, sor_blocking=1, solver_blocks=4)) as cav:
+        rc, steps = cav.step(2)
+    assert rc == 0 and all(s["status"] == 0 for s in steps)
 @pytest.mark.parametrize("blocking", BLOCKING)
 @pytest.mark.parametrize("itmax", [2, 9])
 def test_itmax_reports_not_converged_and_stops(cnv, blocking, itmax):
