@@ -37,8 +37,11 @@ int time_probe(int sms, double* out, double* ops_per_s) {
     const int blocks = sms * 8;
     const int iters = 4096;
     const double ops = (double)blocks * kProbeThreads * iters * kChains * (FMA ? 1 : 2);
-    cudaEvent_t e0, e1;
-    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return CNV_CUDA_ERROR;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return CNV_CUDA_ERROR;
+    }
     float best = 1e30f;
     for (int rep = 0; rep < 4; ++rep) {  // the first run warms up
         cudaEventRecord(e0);
