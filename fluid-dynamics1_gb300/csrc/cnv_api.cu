@@ -108,6 +108,7 @@ struct cnv_state {
     double* alt[2] = {nullptr, nullptr};
     double* rhs[2] = {nullptr, nullptr};
     double* scratch = nullptr;   // 2*n*n: right-hand side and result of standalone Poisson solves
+    double* stage = nullptr;     // 3*n*n: host fields uploaded by cnv_set_fields, checked on the device
     void* sync = nullptr;        // Poisson solver synchronisation state
     // mixed-precision form (CNV_PREC_MIXED)
     bool mixed = false;
@@ -158,7 +159,7 @@ void free_state(cnv_state* s) {
         for (auto& g : row)
             if (g) cudaGraphExecDestroy(g);
     double* bufs[] = {s->w[0], s->w[1], s->u, s->v, s->psi, s->sor[0], s->sor[1], s->alt[0],
-                      s->alt[1], s->rhs[0], s->rhs[1], s->scratch, s->cont_partials};
+                      s->alt[1], s->rhs[0], s->rhs[1], s->scratch, s->stage, s->cont_partials};
     for (double* b : bufs)
         if (b) cudaFree(b);
     for (float* b : {s->rq, s->eg})
@@ -683,14 +684,19 @@ int check_finite_host(const double* x, size_t count) {
 int cnv_set_fields(cnv_state* s, const double* w, const double* u, const double* v) {
     if (!s) return fail(CNV_BAD_ARG, "null state");
     const size_t nn = (size_t)s->n * s->n;
-    for (const double* x : {w, u, v})
-        if (x && !check_finite_host(x, nn)) return fail(CNV_NONFINITE, "input field holds NaN or Inf");
     CNV_CUDA(cudaSetDevice(s->device));
-    if (w) CNV_CUDA(cudaMemcpyAsync(s->w[s->cur], w, nn * 8, cudaMemcpyHostToDevice, s->stream));
-    if (u) CNV_CUDA(cudaMemcpyAsync(s->u, u, nn * 8, cudaMemcpyHostToDevice, s->stream));
-    if (v) CNV_CUDA(cudaMemcpyAsync(s->v, v, nn * 8, cudaMemcpyHostToDevice, s->stream));
-    CNV_CUDA(cudaStreamSynchronize(s->stream));
-    return CNV_OK;
+    // upload into a staging area and check there (a device scan costs microseconds where a host
+    // scan of 3 n^2 doubles costs about a millisecond at 1024^2); the state changes only if
+    // every field is finite
+    if (!s->stage) CNV_CUDA(cudaMalloc(&s->stage, 3 * nn * sizeof(double)));
+    const double* src[3] = {w, u, v};
+    const double* dev[3] = {nullptr, nullptr, nullptr};
+    for (int k = 0; k < 3; ++k) {
+        if (!src[k]) continue;
+        CNV_CUDA(cudaMemcpyAsync(s->stage + k * nn, src[k], nn * 8, cudaMemcpyHostToDevice, s->stream));
+        dev[k] = s->stage + k * nn;
+    }
+    return cnv_set_fields_device(s, dev[0], dev[1], dev[2]);
 }
 
 int cnv_get_fields(cnv_state* s, double* w, double* u, double* v, double* psi) {

@@ -283,11 +283,18 @@ def test_solver_choice_and_geometry(cnv, n, kw, want):
 def test_nonfinite_input_rejected(cnv):
     cfg = make_cfg(cnv, 16)
     with cnv.Cavity(cfg) as cav:
+        before = cav.get_fields()
         w = np.zeros((16, 16))
         w[3, 4] = np.nan
         assert cav.set_fields(w=w) == cnv.CNV_NONFINITE
         w[3, 4] = np.inf
         assert cav.set_fields(w=w) == cnv.CNV_NONFINITE
+        # a finite field next to a non-finite one is not applied either: the state is untouched
+        v = np.zeros((16, 16))
+        v[0, 0] = -np.inf
+        assert cav.set_fields(u=np.full((16, 16), 0.5), v=v) == cnv.CNV_NONFINITE
+        for a, b in zip(cav.get_fields(), before):
+            assert bitwise(a, b)
         rc, steps = cav.step(1)
         assert rc == 0
 
