@@ -673,14 +673,6 @@ int cnv_reset(cnv_state* s) {
 
 int cnv_grid_size(const cnv_state* s) { return s ? s->n : -1; }
 
-namespace {
-int check_finite_host(const double* x, size_t count) {
-    for (size_t k = 0; k < count; ++k)
-        if (!std::isfinite(x[k])) return 0;
-    return 1;
-}
-}  // namespace
-
 int cnv_set_fields(cnv_state* s, const double* w, const double* u, const double* v) {
     if (!s) return fail(CNV_BAD_ARG, "null state");
     const size_t nn = (size_t)s->n * s->n;
@@ -855,9 +847,15 @@ int cnv_poisson_device(cnv_state* s, const double* f, double* psi_out, int* iter
 int cnv_poisson(cnv_state* s, const double* f, double* psi, int* iters, double* err) {
     if (!s || !f || !psi) return fail(CNV_BAD_ARG, "null argument");
     const size_t nn = (size_t)s->n * s->n;
-    if (!check_finite_host(f, nn)) return fail(CNV_NONFINITE, "right-hand side holds NaN or Inf");
     CNV_CUDA(cudaSetDevice(s->device));
     CNV_CUDA(cudaMemcpyAsync(s->scratch, f, nn * 8, cudaMemcpyHostToDevice, s->stream));
+    // reject a non-finite right-hand side before solving (scanned on the device)
+    CNV_CUDA(cudaMemsetAsync(s->flag, 0, sizeof(int), s->stream));
+    CNV_CUDA(launch_nonfinite_scan(s->scratch, (long long)nn, s->flag, s->stream));
+    int bad = 0;
+    CNV_CUDA(cudaMemcpyAsync(&bad, s->flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    CNV_CUDA(cudaStreamSynchronize(s->stream));
+    if (bad) return fail(CNV_NONFINITE, "right-hand side holds NaN or Inf");
     int rc = cnv_poisson_device(s, s->scratch, s->scratch + nn, iters, err);
     CNV_CUDA(cudaMemcpyAsync(psi, s->scratch + nn, nn * 8, cudaMemcpyDeviceToHost, s->stream));
     CNV_CUDA(cudaStreamSynchronize(s->stream));

@@ -295,6 +295,10 @@ def test_nonfinite_input_rejected(cnv):
         assert cav.set_fields(u=np.full((16, 16), 0.5), v=v) == cnv.CNV_NONFINITE
         for a, b in zip(cav.get_fields(), before):
             assert bitwise(a, b)
+        # the standalone solve rejects a non-finite right-hand side before solving
+        f = np.ones((16, 16))
+        f[5, 5] = np.nan
+        assert cav.poisson(f)[0] == cnv.CNV_NONFINITE
         rc, steps = cav.step(1)
         assert rc == 0
 
