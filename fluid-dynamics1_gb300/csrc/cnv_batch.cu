@@ -35,6 +35,7 @@
 
 #include "cnv_kernels.h"
 #include "cnv_stencil.cuh"
+#include "cnv_sync.cuh"
 
 namespace cnv {
 
@@ -94,7 +95,6 @@ namespace {
 
 constexpr int kMaxBatchThreads = 1024;
 
-__device__ __forceinline__ int floor_half(int j) { return j >= 0 ? j / 2 : -((1 - j) / 2); }
 
 // Block-wide sum of a double (deterministic: xor butterfly, then warps in order).
 __device__ double block_sum(double x, double* s_red) {
@@ -281,18 +281,6 @@ __device__ int batch_step(CavityDesc& C, float* smem, int max_outer, double rtol
 constexpr int kStripSweeps = 4;                // FP32 sweeps between border exchanges (8: 1 % faster, more smem)
 constexpr int kStripHalo = 2 * kStripSweeps;   // halo rows of a strip
 
-__device__ __forceinline__ unsigned bt_ld_acquire(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ long long bt_now() {
-    long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 // Barrier of the g blocks of a group (counter gs->bar, target gen). False if the wait gave up
 // (2 s; sets *abort = CNV_TIMEOUT) or another block has aborted; the caller leaves the job.
 __device__ bool group_barrier(GroupSync* gs, unsigned& gen, int g, int* abort, int* s_ok) {
@@ -303,13 +291,13 @@ __device__ bool group_barrier(GroupSync* gs, unsigned& gen, int g, int* abort, i
         atomicAdd(&gs->bar, 1u);
         int ok = 1, polls = 0;
         long long t0 = 0;
-        while ((int)(bt_ld_acquire(&gs->bar) - gen) < 0) {
+        while ((int)(ld_acquire(&gs->bar) - gen) < 0) {
             if (*(volatile int*)abort) {
                 ok = 0;
                 break;
             }
-            if (++polls == 64) t0 = bt_now();
-            if (polls > 64 && bt_now() - t0 > 2000000000LL) {
+            if (++polls == 64) t0 = globaltimer_ns();
+            if (polls > 64 && globaltimer_ns() - t0 > 2000000000LL) {
                 atomicExch(abort, CNV_TIMEOUT);
                 ok = 0;
                 break;

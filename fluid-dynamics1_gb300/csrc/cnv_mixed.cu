@@ -35,6 +35,7 @@
 
 #include "cnv_kernels.h"
 #include "cnv_stencil.cuh"
+#include "cnv_sync.cuh"
 
 namespace cnv {
 namespace {
@@ -50,37 +51,6 @@ struct MixedSync {
     double partial[2][kMaxSolverBlocks];  // per-block ||R||^2 and ||g||^2
     unsigned int flag[kMaxSolverBlocks];  // last epoch whose border strips a block has written
 };
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-__device__ __forceinline__ long long globaltimer_ns() {
-    long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ bool wait_geq(const unsigned* p, unsigned want, Ctrl* ctl, long long timeout_ns) {
-    long long t0 = 0;
-    int polls = 0;
-    while ((int)(ld_acquire(p) - want) < 0) {
-        if (*(const volatile int*)&ctl->abort) return false;
-        if (++polls == 64) t0 = globaltimer_ns();
-        if (polls > 64 && globaltimer_ns() - t0 > timeout_ns) {
-            atomicExch(&ctl->status, CNV_TIMEOUT);
-            atomicExch(&ctl->abort, 1);
-            return false;
-        }
-    }
-    return true;
-}
 
 // Grid-wide barrier (counter of arrivals); false if it timed out or another block aborted.
 __device__ bool grid_sync(MixedSync* sy, unsigned& epoch, Ctrl* ctl, long long timeout_ns, int* s_ok) {
@@ -118,8 +88,6 @@ __device__ __forceinline__ MTile make_mtile(int n, int gx, int gy, int b) {
         }
     return t;
 }
-
-__host__ __device__ __forceinline__ int floor_half(int j) { return j >= 0 ? j / 2 : -((1 - j) / 2); }
 
 // Shared-memory tile in split layout: rows sr0 .. sr0+sh-1, global split columns m0 .. m0+swm-1.
 struct SmemTile {

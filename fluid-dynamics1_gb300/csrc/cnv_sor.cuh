@@ -1,47 +1,14 @@
 // cnv_sor.cuh -- device pieces shared by the persistent SOR kernels (cnv_poisson.cu,
-// cnv_poisson_tb.cu): inter-block signalling with bounded waits, the exact fixed-point stop
-// norm, and the point update of src/poisson.c:247 in its three arithmetic forms. Both kernels
+// cnv_poisson_tb.cu): the exact fixed-point stop norm, the exact multiply by a constant, and
+// the point update of src/poisson.c:247 in its three arithmetic forms. Both kernels
 // use these same functions so that they produce the same bits.
 #pragma once
 
 #include "cnv_kernels.h"
+#include "cnv_sync.cuh"
 
 namespace cnv {
 namespace {
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-__device__ __forceinline__ long long globaltimer_ns() {
-    long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ int ld_volatile_int(const int* p) { return *(const volatile int*)p; }
-
-// Wait until *p >= want (as sweep counters). Returns false on timeout or abort.
-__device__ bool wait_geq(const unsigned* p, unsigned want, Ctrl* ctl, long long timeout_ns) {
-    long long t0 = 0;
-    int polls = 0;
-    while ((int)(ld_acquire(p) - want) < 0) {
-        if (ld_volatile_int(&ctl->abort)) return false;
-        if (++polls == 64) t0 = globaltimer_ns();
-        if (polls > 64 && globaltimer_ns() - t0 > timeout_ns) {
-            atomicExch(&ctl->status, CNV_TIMEOUT);
-            atomicExch(&ctl->abort, 1);
-            return false;
-        }
-    }
-    return true;
-}
 
 // exact 128-bit fixed-point image (scale 2^80, truncated) of a non-negative double
 __device__ __forceinline__ void to_fixed96(double x, unsigned long long& lo, unsigned long long& hi) {
