@@ -5,6 +5,8 @@
   byte for byte; cnv_write_vtk writes src/utils.c's VTK layout byte for byte.
 - cnavier_gpu run on the configurations of the reference's shipped red-black logs reproduces
   every logged step: iteration count, stop norm and continuity max/min as printed.
+- The reference's own program sources, compiled where they lie, link against the compatibility
+  library in place of src/poisson.c and src/fluiddyn.c (both builds; CPU only).
 - The compatibility library's euler() and poisson_SOR_log(), driven by a copy of the
   reference's time loop (src/main.c:283-383) whose derivative products come from the oracle,
   give the oracle's fields bit for bit; cnavier_gpu's VTK files hold the oracle's fields.
@@ -132,6 +134,31 @@ def test_program_writes_reference_vtk_files(tmp_path, orc):
     assert orc.run(p, 7, W, U, V, PSI)[0] == 0  # the files of step 6 (the last ones)
     for k, field in zip(range(8, 12), (PSI, W, U, V)):
         assert open(tmp_path / "output" / "vtk" / f"{titles[k % 4]}-1-{k}.vtk").read() == reference_vtk(field)
+
+
+# ------------------------------------------------------- the compatibility library, linked (CPU)
+def test_reference_program_links_against_compat_library():
+    """The reference's own main.c, linearalg.c, finitediff.c, utils.c and config.c, compiled where
+    they lie (oracle/Makefile, target ab), link against libcnv_compat.so + libcnv.so in place of
+    src/poisson.c and src/fluiddyn.c, in both of the reference's builds: the compatibility library
+    defines every function the program takes from those two files. The programs only print their
+    usage here (no GPU)."""
+    ref = os.environ.get("CNV_REFERENCE_TREE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "src")):
+        pytest.skip("reference tree absent")
+    import build as product_build  # fluid-dynamics1_gb300/build.py
+
+    product_build.build()
+    oracle_dir = os.path.join(ROOT, "oracle")
+    subprocess.run(["make", "-s", "-B", "-C", oracle_dir, "ab", f"REF={ref}", f"LIBCNV={PKG}"], check=True)
+    for exe in ("cnavier_ab", "cnavier_ab_seq"):
+        path = os.path.join(oracle_dir, "_ref", exe)
+        undefined = subprocess.run(["nm", "-D", "--undefined-only", path], capture_output=True, text=True,
+                                   check=True).stdout.split()
+        for name in ("euler", "poisson_SOR_log", "poisson_log", "continuity"):
+            assert name in undefined, (exe, name)  # taken from the library, not compiled in
+        r = subprocess.run([path, "--help"], capture_output=True, text=True, timeout=60)
+        assert r.returncode == 0 and r.stdout.startswith("Usage:"), (exe, r.stdout[:200], r.stderr[:200])
 
 
 # --------------------------------------------------------------- the compatibility library (GPU)
