@@ -354,6 +354,7 @@ def form_batched(cnvpy, local, steps, count=256, seed=0):
         sample.append(next(k for k, s in enumerate(specs) if s["n"] == n))
     with cnvpy.Batch(base, specs) as bt:
         threads, per_sm = bt.tune()
+        groups = bt.groups()
         bt.step(1)
         rc, last = bt.step(steps)
         cells, sweeps, ms = bt.stats()
@@ -361,6 +362,8 @@ def form_batched(cnvpy, local, steps, count=256, seed=0):
     out["batched"] = {"value": mcells(cells, steps, ms), "unit": UNIT, "steps": steps, "cells": cells,
                       "ms_per_step": round(ms / steps, 3), "tuned_shape": {"threads": threads,
                                                                            "blocks_per_sm": per_sm},
+                      "blocks_per_cavity": {str(n): groups[sample[i]] for i, n in
+                                            enumerate(sorted({s["n"] for s in specs}))},
                       "max_relative_residual": max(x["err"] for x in last)}
     f_cells, f_ms, errs = 0, 0.0, {}
     for k in sample:

@@ -612,6 +612,7 @@ struct cnv_batch {
     int* abort = nullptr;          // group-wait failure flag (device)
     int split = 1;                 // strips per cavity beyond what shared memory needs
     int split_min_n = 256;         // ... for cavities of at least this many points per side
+    std::vector<std::pair<int, int>> group_by_n;  // (n, group) chosen by the cost model; empty: rule above
     int* nsteps = nullptr;
     int threads = 1024;
     int blocks = 0;
@@ -648,24 +649,23 @@ inline unsigned long long mix64(unsigned long long z) {
 }
 
 // Row strips a cavity needs so that one strip's FP32 correction (plus halo rows) fits a block's
-// shared memory: 1 if the whole cavity's correction fits, else the smallest power of two that
-// does (strips at least 2 halos high); then `split` times more for cavities of at least min_n
-// points. 0 if no decomposition fits.
-int group_size(int n, int smem_bytes, int split, int min_n) {
+// shared memory: 1 if the whole cavity's correction fits, else the smallest count that does
+// (strips at least 2 halos high). 0 if no decomposition fits.
+int min_group(int n, int smem_bytes) {
     const size_t sp = (size_t)(n + 1) / 2 + 1;
-    int g = 0;
-    if (2 * (size_t)n * sp * 4 <= (size_t)smem_bytes) {
-        g = 1;
-    } else {
-        for (int t = 2; t <= kMaxGroup; t *= 2) {
-            const size_t rows = (size_t)(n + t - 1) / t + 2 * kStripHalo;
-            if (n / t >= 2 * kStripHalo && 2 * rows * sp * 4 <= (size_t)smem_bytes) {
-                g = t;
-                break;
-            }
-        }
-        if (!g) return 0;
+    if (2 * (size_t)n * sp * 4 <= (size_t)smem_bytes) return 1;
+    for (int t = 2; t <= kMaxGroup && n / t >= 2 * kStripHalo; ++t) {
+        const size_t rows = (size_t)(n + t - 1) / t + 2 * kStripHalo;
+        if (2 * rows * sp * 4 <= (size_t)smem_bytes) return t;
     }
+    return 0;
+}
+
+// min_group, then `split` times more (doubling while the strips stay 2 halos high) for cavities
+// of at least min_n points. 0 if no decomposition fits.
+int group_size(int n, int smem_bytes, int split, int min_n) {
+    int g = min_group(n, smem_bytes);
+    if (!g) return 0;
     if (n >= min_n)
         while (split > 1 && g * 2 <= kMaxGroup && n / (g * 2) >= 2 * kStripHalo) {
             g *= 2;
@@ -731,37 +731,47 @@ int build_graph(cnv_batch* b) {
     return CNV_OK;
 }
 
-// Job lists: cavities largest estimated cost first, each on the `group` blocks that become free
-// first; every block's list in start-time order (so groups meet in one global order).
-int build_schedule(cnv_batch* b) {
-    const int nb = b->blocks;
-    std::vector<int> idx(b->count);
+// Greedy placement of one step's jobs: cavities largest estimated cost first, each on the
+// `group` blocks that become free first. Fills the per-block lists (start-time order) when asked;
+// returns the estimated makespan (microseconds).
+struct Placed {
+    double start;
+    int cav, rank, group;
+};
+
+double place_jobs(const std::vector<CavityDesc>& desc, int nb, std::vector<std::vector<Placed>>* lists) {
+    const int count = (int)desc.size();
+    std::vector<int> idx(count);
     std::iota(idx.begin(), idx.end(), 0);
-    std::vector<double> cost(b->count);
-    for (int k = 0; k < b->count; ++k) {
-        const CavityDesc& d = b->host_desc[k];
-        cost[k] = step_cost(d.n, d.group, d.smem_mode);
-    }
+    std::vector<double> cost(count);
+    for (int k = 0; k < count; ++k) cost[k] = step_cost(desc[k].n, desc[k].group, desc[k].smem_mode);
     std::stable_sort(idx.begin(), idx.end(), [&](int a, int c) { return cost[a] > cost[c]; });
     std::vector<double> avail(nb, 0.0);
-    struct Placed {
-        double start;
-        int cav, rank, group;
-    };
-    std::vector<std::vector<Placed>> lists(nb);
     std::vector<int> blocks(nb);
     for (int k : idx) {
-        const int g = b->host_desc[k].group;
-        if (g > nb) return bfail(CNV_BAD_ARG, "a cavity needs more blocks than the device runs at once");
+        const int g = desc[k].group;
         std::iota(blocks.begin(), blocks.end(), 0);
-        std::stable_sort(blocks.begin(), blocks.end(), [&](int a, int c) { return avail[a] < avail[c]; });
+        std::partial_sort(blocks.begin(), blocks.begin() + g, blocks.end(), [&](int a, int c) {
+            return avail[a] < avail[c] || (avail[a] == avail[c] && a < c);
+        });
         double start = 0.0;
         for (int r = 0; r < g; ++r) start = std::max(start, avail[blocks[r]]);
         for (int r = 0; r < g; ++r) {
-            lists[blocks[r]].push_back(Placed{start, k, r, g});
+            if (lists) (*lists)[blocks[r]].push_back(Placed{start, k, r, g});
             avail[blocks[r]] = start + cost[k];
         }
     }
+    return *std::max_element(avail.begin(), avail.end());
+}
+
+// Job lists of the current decomposition (see place_jobs), on the device; every block's list in
+// start-time order, so the blocks of a group reach their common jobs in one global order.
+int build_schedule(cnv_batch* b) {
+    const int nb = b->blocks;
+    for (const auto& d : b->host_desc)
+        if (d.group > nb) return bfail(CNV_BAD_ARG, "a cavity needs more blocks than the device runs at once");
+    std::vector<std::vector<Placed>> lists(nb);
+    b->makespan_us = place_jobs(b->host_desc, nb, &lists);
     std::vector<SchedEntry> flat;
     std::vector<int> off(nb + 1, 0);
     for (int q = 0; q < nb; ++q) {
@@ -779,8 +789,50 @@ int build_schedule(cnv_batch* b) {
     if (!flat.empty())
         BCUDA(cudaMemcpy(b->sched, flat.data(), sizeof(SchedEntry) * flat.size(), cudaMemcpyHostToDevice));
     BCUDA(cudaMemcpy(b->sched_off, off.data(), sizeof(int) * (nb + 1), cudaMemcpyHostToDevice));
-    b->makespan_us = *std::max_element(avail.begin(), avail.end());
     return CNV_OK;
+}
+
+// Group sizes chosen by the cost model: every distinct cavity size whose correction needs row
+// strips gets a group from the smallest that fits to three more (strips at least 2 halos high),
+// the sizes tried jointly (the three largest such sizes; smaller ones keep the smallest group),
+// and the combination with the smallest estimated makespan is kept in b->group_by_n.
+void model_groups(cnv_batch* b) {
+    std::vector<int> sizes;
+    for (const auto& d : b->host_desc)
+        if (min_group(d.n, b->smem_bytes) >= 2 && std::find(sizes.begin(), sizes.end(), d.n) == sizes.end())
+            sizes.push_back(d.n);
+    std::sort(sizes.rbegin(), sizes.rend());
+    if (sizes.size() > 3) sizes.resize(3);
+    std::vector<std::vector<int>> opts;
+    for (int n : sizes) {
+        std::vector<int> o;
+        const int g0 = min_group(n, b->smem_bytes);
+        for (int g = g0; g <= g0 + 3 && g <= kMaxGroup && g <= b->blocks && n / g >= 2 * kStripHalo; ++g) o.push_back(g);
+        opts.push_back(o);
+    }
+    std::vector<CavityDesc> desc = b->host_desc;
+    std::vector<int> pick(sizes.size(), 0), best_pick = pick;
+    double best = 1e300;
+    for (;;) {
+        for (auto& d : desc) {
+            const size_t plane = (size_t)d.n * d.spitch * 4;
+            d.smem_mode = 4 * plane <= (size_t)b->smem_bytes ? 2 : 2 * plane <= (size_t)b->smem_bytes ? 1 : 0;
+            d.group = std::max(1, min_group(d.n, b->smem_bytes));
+            for (size_t q = 0; q < sizes.size(); ++q)
+                if (d.n == sizes[q]) d.group = opts[q][pick[q]];
+            if (d.group > 1) d.smem_mode = 1;
+        }
+        const double ms = place_jobs(desc, b->blocks, nullptr);
+        if (ms < best) {
+            best = ms;
+            best_pick = pick;
+        }
+        size_t q = 0;  // next combination
+        while (q < sizes.size() && ++pick[q] == (int)opts[q].size()) pick[q++] = 0;
+        if (q == sizes.size()) break;
+    }
+    b->group_by_n.clear();
+    for (size_t q = 0; q < sizes.size(); ++q) b->group_by_n.emplace_back(sizes[q], opts[q][best_pick[q]]);
 }
 
 // Launch shape: threads per block and blocks per SM; shared memory as the SM allows; the strip
@@ -802,6 +854,8 @@ int set_shape(cnv_batch* b, int threads, int per_sm) {
         const size_t plane = (size_t)d.n * d.spitch * 4;
         d.smem_mode = 4 * plane <= (size_t)b->smem_bytes ? 2 : 2 * plane <= (size_t)b->smem_bytes ? 1 : 0;
         d.group = group_size(d.n, b->smem_bytes, b->split, b->split_min_n);
+        for (const auto& ng : b->group_by_n)
+            if (ng.first == d.n && d.group > 0) d.group = ng.second;
         if (d.group == 0) d.group = 1;  // no strip decomposition fits: one block, correction in L2
         if (d.group > 1) d.smem_mode = 1;
     }
@@ -989,16 +1043,24 @@ int cnv_batch_tune(cnv_batch* b, int* threads_out, int* blocks_per_sm_out) {
     if (!b) return bfail(CNV_BAD_ARG, "null batch");
     BCUDA(cudaSetDevice(b->device));
     // candidates: row-strip decompositions (strips only where shared memory needs them, or 2x or
-    // 4x as many for the largest cavities), each timed for one step from the initial state, on
-    // one block of 1024 threads per SM (the shared-memory tiles need the whole SM)
-    const int cand[][2] = {{1, 256}, {2, 256}, {4, 256}, {2, 192}};
+    // 4x as many for the largest cavities, or the groups the cost model picks), each timed for
+    // one step from the initial state, on one block of 1024 threads per SM (the shared-memory
+    // tiles need the whole SM)
+    const int cand[][3] = {{1, 256, 0}, {2, 256, 0}, {4, 256, 0}, {2, 192, 0}, {1, 256, 1}};
     double best = 1e300;
     int bs = 1, bm = 256;
+    std::vector<std::pair<int, int>> bg;
     for (const auto& c : cand) {
         b->split = c[0];
         b->split_min_n = c[1];
+        b->group_by_n.clear();
         int rc = set_shape(b, 1024, 1);
         if (rc != CNV_OK) continue;
+        if (c[2]) {
+            model_groups(b);
+            rc = set_shape(b, 1024, 1);
+            if (rc != CNV_OK) continue;
+        }
         rc = reset_fields(b);
         if (rc == CNV_OK) rc = run(b, 1);
         if (rc != CNV_OK) return rc;
@@ -1006,10 +1068,12 @@ int cnv_batch_tune(cnv_batch* b, int* threads_out, int* blocks_per_sm_out) {
             best = b->last_ms;
             bs = c[0];
             bm = c[1];
+            bg = b->group_by_n;
         }
     }
     b->split = bs;
     b->split_min_n = bm;
+    b->group_by_n = bg;
     int rc = set_shape(b, 1024, 1);
     if (rc == CNV_OK) rc = reset_fields(b);
     if (threads_out) *threads_out = b->threads;
@@ -1022,6 +1086,7 @@ int cnv_batch_split(cnv_batch* b, int factor, int min_n) {
     BCUDA(cudaSetDevice(b->device));
     b->split = factor;
     b->split_min_n = min_n;
+    b->group_by_n.clear();
     int rc = set_shape(b, 1024, 1);
     if (rc == CNV_OK) rc = reset_fields(b);
     return rc;

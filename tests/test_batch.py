@@ -138,6 +138,27 @@ def test_row_strip_groups_equal_single_cavity_runs(cnv):
 
 
 @pytest.mark.gpu
+def test_tuned_groups_on_large_cavities_equal_single_runs(cnv):
+    """The tuner's candidates include group sizes picked by the cost model (any strip count, not
+    only powers of two); whichever it keeps, every cavity equals its single-cavity run."""
+    specs = [dict(n=384, Re=1500.0, lid=1.2), dict(n=384, Re=200.0, lid=0.6), dict(n=256, Re=300.0, lid=0.7),
+             dict(n=256, Re=1900.0, lid=1.4), dict(n=96, Re=900.0, lid=1.0)]
+    base = cnv.default_config(mixed_rtol=1e-10)
+    nsteps = 2
+    with cnv.Batch(base, specs) as bt:
+        bt.tune()
+        groups = bt.groups()
+        rc, last = bt.step(nsteps)
+        fields = [bt.get_fields(k) for k in range(len(specs))]
+    assert rc == 0 and min(groups[:2]) >= 3 and min(groups[2:4]) >= 2, groups
+    for k, sp in enumerate(specs):
+        steps, single = _single_mixed(cnv, sp, nsteps)
+        assert last[k]["iters"] == steps[-1]["iters"], k
+        for name, a, b in zip("w u v psi".split(), fields[k], single):
+            assert np.max(np.abs(a - b)) <= SAME_SCHEME_TOL * np.max(np.abs(b)), (k, name)
+
+
+@pytest.mark.gpu
 def test_large_cavities_on_their_default_strips(cnv):
     specs = [dict(n=384, Re=1500.0, lid=1.2), dict(n=256, Re=300.0, lid=0.7), dict(n=192, Re=900.0, lid=1.0)]
     base = cnv.default_config(mixed_rtol=1e-10)
@@ -146,7 +167,8 @@ def test_large_cavities_on_their_default_strips(cnv):
         groups = bt.groups()
         rc, last = bt.step(nsteps)
         fields = [bt.get_fields(k) for k in range(len(specs))]
-    assert rc == 0 and groups[0] > 1 and groups[1] > 1
+    # a 384^2 correction needs 3 strips of a GB300 block's shared memory, 256^2 needs 2
+    assert rc == 0 and groups == [3, 2, 1]
     for k, sp in enumerate(specs):
         steps, single = _single_mixed(cnv, sp, nsteps)
         assert last[k]["iters"] == steps[-1]["iters"], k
