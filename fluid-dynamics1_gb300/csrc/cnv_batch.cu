@@ -23,7 +23,8 @@
 // no wait can close a cycle. The launch is cooperative (all blocks resident), captured in a CUDA
 // graph with the per-launch counters reset, and reads the step count from device memory so one
 // graph serves every call. The autotuner (cnv_batch_tune) times one step of each candidate
-// decomposition (strips only where shared memory needs them, or more) and keeps the fastest.
+// decomposition (strips only where shared memory needs them, or more, or the strip counts per
+// cavity size that minimise the schedule's estimated makespan) and keeps the fastest.
 #include <algorithm>
 #include <cfloat>
 #include <cmath>

@@ -216,8 +216,9 @@ int cnv_batch_create(const cnv_config *base, int count, const cnv_cavity_spec *s
 void cnv_batch_destroy(cnv_batch *b);
 int cnv_batch_reset(cnv_batch *b);
 /* Time one step of each candidate decomposition (row strips only where shared memory needs
- * them, or 2x / 4x as many for the largest cavities) from the initial state, keep the fastest,
- * and reset the fields. Reports the launch shape (threads per block, blocks per SM); either
+ * them, 2x / 4x as many for the largest cavities, or the strip counts per cavity size that a
+ * cost model of the schedule picks) from the initial state, keep the fastest, and reset the
+ * fields. Reports the launch shape (threads per block, blocks per SM); either
  * pointer may be NULL. */
 int cnv_batch_tune(cnv_batch *b, int *threads, int *blocks_per_sm);
 /* Use factor times more row strips than shared memory needs for cavities of at least min_n
