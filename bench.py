@@ -601,6 +601,7 @@ def only(args):
                        poisson_type=ptype)
         elif name == "batched":
             with cnvpy.Batch(cnvpy.default_config(mixed_rtol=1e-10), cnvpy.batch_specs(256, seed=0)) as bt:
+                bt.tune()  # one launch per candidate decomposition (5), then the step on the kept one
                 bt.step(1)
         elif name == "adjoint":
             n = 256
