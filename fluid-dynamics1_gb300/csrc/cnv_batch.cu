@@ -1011,8 +1011,13 @@ int cnv_batch_create(const cnv_config* base, int count, const cnv_cavity_spec* s
     }
     if (cudaMemcpy(b->bands, hb.data(), sizeof(FdBands) * count, cudaMemcpyHostToDevice) != cudaSuccess)
         return cleanup(CNV_CUDA_ERROR, "descriptor upload failed");
+    // the strip counts the cost model picks (set_shape first gives it the launch shape)
     int rc = reset_fields(b);
     if (rc == CNV_OK) rc = set_shape(b, 1024, 1);
+    if (rc == CNV_OK) {
+        model_groups(b);
+        rc = set_shape(b, 1024, 1);
+    }
     if (rc != CNV_OK) {
         cnv_batch_destroy(b);
         return rc;

@@ -211,7 +211,9 @@ typedef struct cnv_batch cnv_batch;
  * Re uniform in [100, 2000], lid uniform in [0.5, 1.5], dt by the stability rule. */
 int cnv_batch_specs(int count, unsigned long long seed, cnv_cavity_spec *out);
 /* Fields start as cnv_create's; base supplies order, Lx/Ly, the other wall velocities and the
- * mixed-form settings. */
+ * mixed-form settings. Cavities whose FP32 correction does not fit one block's shared memory run
+ * as row strips on a group of blocks, with the strip counts per cavity size that minimise a cost
+ * model of the schedule's makespan (cnv_batch_split(b, 1, n) asks for the smallest counts). */
 int cnv_batch_create(const cnv_config *base, int count, const cnv_cavity_spec *specs, cnv_batch **out);
 void cnv_batch_destroy(cnv_batch *b);
 int cnv_batch_reset(cnv_batch *b);

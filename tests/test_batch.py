@@ -159,16 +159,19 @@ def test_tuned_groups_on_large_cavities_equal_single_runs(cnv):
 
 
 @pytest.mark.gpu
-def test_large_cavities_on_their_default_strips(cnv):
+def test_large_cavities_on_their_smallest_strips(cnv):
     specs = [dict(n=384, Re=1500.0, lid=1.2), dict(n=256, Re=300.0, lid=0.7), dict(n=192, Re=900.0, lid=1.0)]
     base = cnv.default_config(mixed_rtol=1e-10)
     nsteps = 2
     with cnv.Batch(base, specs) as bt:
+        model = bt.groups()  # the cost model's counts: at least the smallest that fit
+        bt.split(1, 256)     # strips only where shared memory needs them
         groups = bt.groups()
         rc, last = bt.step(nsteps)
         fields = [bt.get_fields(k) for k in range(len(specs))]
     # a 384^2 correction needs 3 strips of a GB300 block's shared memory, 256^2 needs 2
     assert rc == 0 and groups == [3, 2, 1]
+    assert all(m >= g for m, g in zip(model, groups)) and model[0] > 3, model
     for k, sp in enumerate(specs):
         steps, single = _single_mixed(cnv, sp, nsteps)
         assert last[k]["iters"] == steps[-1]["iters"], k
