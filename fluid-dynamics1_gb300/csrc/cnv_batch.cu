@@ -705,8 +705,8 @@ int build_graph(cnv_batch* b) {
     BCUDA(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, b->smem_bytes));
     cudaGraph_t g = nullptr;
     BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    cudaMemsetAsync(b->gsync, 0, sizeof(GroupSync) * b->count, b->stream);
-    cudaMemsetAsync(b->abort, 0, sizeof(int), b->stream);
+    cudaError_t me = cudaMemsetAsync(b->gsync, 0, sizeof(GroupSync) * b->count, b->stream);
+    if (me == cudaSuccess) me = cudaMemsetAsync(b->abort, 0, sizeof(int), b->stream);
     // cooperative: the blocks of a group wait for one another, so all must be resident
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(b->blocks);
@@ -719,7 +719,8 @@ int build_graph(cnv_batch* b) {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     void* args[] = {&L};
-    const cudaError_t le = cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_batch), args);
+    const cudaError_t le =
+        me != cudaSuccess ? me : cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_batch), args);
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (le != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
