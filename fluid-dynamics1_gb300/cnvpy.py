@@ -94,6 +94,7 @@ _SIGS = {
     "cnv_batch_step": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(StepInfo)]),
     "cnv_batch_split": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "cnv_batch_groups": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "cnv_batch_plan": (C.c_int, [C.c_int, C.POINTER(CavitySpec), C.c_int, C.c_int, C.POINTER(C.c_int), _dp]),
     "cnv_batch_get_fields": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp]),
     "cnv_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),
     "cnv_adjoint_create": (C.c_int, [C.POINTER(Config), C.c_int, C.POINTER(C.c_void_p)]),
@@ -267,6 +268,17 @@ def batch_specs(count: int, seed: int = 0):
     arr = (CavitySpec * count)()
     check(load().cnv_batch_specs(count, seed, arr), "cnv_batch_specs")
     return [dict(n=a.n, Re=a.Re, lid=a.lid, dt=a.dt) for a in arr]
+
+
+def batch_plan(specs, blocks: int = 152, smem_bytes: int = 231424):
+    """cnv_batch_plan (host only): the row strips per cavity that a batch of these cavities gets on
+    a device running `blocks` blocks of `smem_bytes` bytes of shared memory (defaults: a GB300),
+    and the schedule's estimated step time in microseconds."""
+    arr = (CavitySpec * len(specs))(*[CavitySpec(s["n"], s["Re"], s["lid"], s.get("dt", 0.0)) for s in specs])
+    groups = (C.c_int * len(specs))()
+    us = C.c_double(0.0)
+    check(load().cnv_batch_plan(len(specs), arr, blocks, smem_bytes, groups, C.byref(us)), "cnv_batch_plan")
+    return list(groups), us.value
 
 
 class Batch:

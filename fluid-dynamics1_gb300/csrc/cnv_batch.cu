@@ -794,37 +794,53 @@ int build_schedule(cnv_batch* b) {
     return CNV_OK;
 }
 
+// The decomposition of every cavity for a shared-memory size: group_size's strips (split times
+// more than needed for cavities of at least split_min_n points), or the (n, group) overrides; the
+// placement of the FP32 correction (smem_mode) to match.
+void assign_groups(std::vector<CavityDesc>& desc, int smem_bytes, int split, int split_min_n,
+                   const std::vector<std::pair<int, int>>& group_by_n) {
+    for (auto& d : desc) {
+        const size_t plane = (size_t)d.n * d.spitch * 4;
+        d.smem_mode = 4 * plane <= (size_t)smem_bytes ? 2 : 2 * plane <= (size_t)smem_bytes ? 1 : 0;
+        d.group = group_size(d.n, smem_bytes, split, split_min_n);
+        for (const auto& ng : group_by_n)
+            if (ng.first == d.n && d.group > 0) d.group = ng.second;
+        if (d.group == 0) d.group = 1;  // no strip decomposition fits: one block, correction in L2
+        if (d.group > 1) d.smem_mode = 1;
+    }
+}
+
 // Group sizes chosen by the cost model: every distinct cavity size whose correction needs row
-// strips gets a group from the smallest that fits to three more (strips at least 2 halos high),
-// the sizes tried jointly (the three largest such sizes; smaller ones keep the smallest group),
-// and the combination with the smallest estimated makespan is kept in b->group_by_n.
-void model_groups(cnv_batch* b) {
+// strips gets a group from the smallest that fits to three more (strips at least 2 halos high,
+// at most `blocks`), the sizes tried jointly (the three largest such sizes; smaller ones keep the
+// smallest group), and the combination with the smallest estimated makespan is returned as
+// (n, group) pairs.
+std::vector<std::pair<int, int>> model_groups(const std::vector<CavityDesc>& in, int smem_bytes, int blocks) {
     std::vector<int> sizes;
-    for (const auto& d : b->host_desc)
-        if (min_group(d.n, b->smem_bytes) >= 2 && std::find(sizes.begin(), sizes.end(), d.n) == sizes.end())
+    for (const auto& d : in)
+        if (min_group(d.n, smem_bytes) >= 2 && std::find(sizes.begin(), sizes.end(), d.n) == sizes.end())
             sizes.push_back(d.n);
     std::sort(sizes.rbegin(), sizes.rend());
     if (sizes.size() > 3) sizes.resize(3);
     std::vector<std::vector<int>> opts;
     for (int n : sizes) {
         std::vector<int> o;
-        const int g0 = min_group(n, b->smem_bytes);
-        for (int g = g0; g <= g0 + 3 && g <= kMaxGroup && g <= b->blocks && n / g >= 2 * kStripHalo; ++g) o.push_back(g);
+        const int g0 = min_group(n, smem_bytes);
+        for (int g = g0; g <= g0 + 3 && g <= kMaxGroup && g <= blocks && n / g >= 2 * kStripHalo; ++g) o.push_back(g);
+        if (o.empty()) o.push_back(g0);  // more than the device runs: build_schedule reports it
         opts.push_back(o);
     }
-    std::vector<CavityDesc> desc = b->host_desc;
+    std::vector<CavityDesc> desc = in;
+    std::vector<std::pair<int, int>> trial;
     std::vector<int> pick(sizes.size(), 0), best_pick = pick;
     double best = 1e300;
     for (;;) {
-        for (auto& d : desc) {
-            const size_t plane = (size_t)d.n * d.spitch * 4;
-            d.smem_mode = 4 * plane <= (size_t)b->smem_bytes ? 2 : 2 * plane <= (size_t)b->smem_bytes ? 1 : 0;
-            d.group = std::max(1, min_group(d.n, b->smem_bytes));
-            for (size_t q = 0; q < sizes.size(); ++q)
-                if (d.n == sizes[q]) d.group = opts[q][pick[q]];
-            if (d.group > 1) d.smem_mode = 1;
-        }
-        const double ms = place_jobs(desc, b->blocks, nullptr);
+        trial.clear();
+        for (size_t q = 0; q < sizes.size(); ++q) trial.emplace_back(sizes[q], opts[q][pick[q]]);
+        assign_groups(desc, smem_bytes, 1, 1, trial);
+        bool fits = true;
+        for (const auto& d : desc) fits = fits && d.group <= blocks;
+        const double ms = fits ? place_jobs(desc, blocks, nullptr) : 1e300;
         if (ms < best) {
             best = ms;
             best_pick = pick;
@@ -833,9 +849,12 @@ void model_groups(cnv_batch* b) {
         while (q < sizes.size() && ++pick[q] == (int)opts[q].size()) pick[q++] = 0;
         if (q == sizes.size()) break;
     }
-    b->group_by_n.clear();
-    for (size_t q = 0; q < sizes.size(); ++q) b->group_by_n.emplace_back(sizes[q], opts[q][best_pick[q]]);
+    std::vector<std::pair<int, int>> out;
+    for (size_t q = 0; q < sizes.size(); ++q) out.emplace_back(sizes[q], opts[q][best_pick[q]]);
+    return out;
 }
+
+void model_groups(cnv_batch* b) { b->group_by_n = model_groups(b->host_desc, b->smem_bytes, b->blocks); }
 
 // Launch shape: threads per block and blocks per SM; shared memory as the SM allows; the strip
 // decomposition and the job lists for it.
@@ -852,15 +871,7 @@ int set_shape(cnv_batch* b, int threads, int per_sm) {
     if (occ < 1) return bfail(CNV_CUDA_ERROR, "batched kernel does not fit on an SM");
     b->blocks = std::min(occ, per_sm) * b->sms;
     // per-cavity placement of the FP32 correction for this shared-memory size, and row strips
-    for (auto& d : b->host_desc) {
-        const size_t plane = (size_t)d.n * d.spitch * 4;
-        d.smem_mode = 4 * plane <= (size_t)b->smem_bytes ? 2 : 2 * plane <= (size_t)b->smem_bytes ? 1 : 0;
-        d.group = group_size(d.n, b->smem_bytes, b->split, b->split_min_n);
-        for (const auto& ng : b->group_by_n)
-            if (ng.first == d.n && d.group > 0) d.group = ng.second;
-        if (d.group == 0) d.group = 1;  // no strip decomposition fits: one block, correction in L2
-        if (d.group > 1) d.smem_mode = 1;
-    }
+    assign_groups(b->host_desc, b->smem_bytes, b->split, b->split_min_n, b->group_by_n);
     BCUDA(cudaMemcpy(b->desc, b->host_desc.data(), sizeof(CavityDesc) * b->count, cudaMemcpyHostToDevice));
     const int rc = build_schedule(b);
     if (rc != CNV_OK) return rc;
@@ -905,6 +916,27 @@ int cnv_batch_specs(int count, unsigned long long seed, cnv_cavity_spec* out) {
         out[k].lid = 0.5 + u3;
         out[k].dt = 0.0;
     }
+    return CNV_OK;
+}
+
+int cnv_batch_plan(int count, const cnv_cavity_spec* specs, int blocks, int smem_bytes, int* groups,
+                   double* makespan_us) {
+    if (count < 1 || !specs || !groups || blocks < 1 || smem_bytes < 1024)
+        return bfail(CNV_BAD_ARG, "bad count, block count or shared-memory size, or null argument");
+    std::vector<CavityDesc> desc(count);
+    for (int k = 0; k < count; ++k) {
+        const int n = specs[k].n;
+        if (n < 4 || n > 4096) return bfail(CNV_BAD_ARG, "cavity " + std::to_string(k) + ": n out of range");
+        std::memset(&desc[k], 0, sizeof(CavityDesc));
+        desc[k].n = n;
+        desc[k].spitch = (n + 1) / 2 + 1;
+    }
+    assign_groups(desc, smem_bytes, 1, 1, model_groups(desc, smem_bytes, blocks));
+    for (int k = 0; k < count; ++k) {
+        if (desc[k].group > blocks) return bfail(CNV_BAD_ARG, "a cavity needs more blocks than the device runs at once");
+        groups[k] = desc[k].group;
+    }
+    if (makespan_us) *makespan_us = place_jobs(desc, blocks, nullptr);
     return CNV_OK;
 }
 

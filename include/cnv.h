@@ -228,6 +228,12 @@ int cnv_batch_tune(cnv_batch *b, int *threads, int *blocks_per_sm);
 int cnv_batch_split(cnv_batch *b, int factor, int min_n);
 /* Blocks (row strips) of each cavity under the current decomposition (count entries). */
 int cnv_batch_groups(cnv_batch *b, int *groups);
+/* Host only, no device needed: the row strips per cavity (groups, count entries) that
+ * cnv_batch_create picks on a device that runs `blocks` batch blocks of `smem_bytes` bytes of
+ * shared memory each (a GB300: 152 and 231424), and the schedule's estimated step time in
+ * microseconds (makespan_us, may be NULL). */
+int cnv_batch_plan(int count, const cnv_cavity_spec *specs, int blocks, int smem_bytes, int *groups,
+                   double *makespan_us);
 /* Advance every cavity nsteps steps in one launch; last (count records or NULL) receives each
  * cavity's last step. */
 int cnv_batch_step(cnv_batch *b, int nsteps, cnv_step_info *last);

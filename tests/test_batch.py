@@ -24,6 +24,34 @@ def test_specs_generator_is_deterministic_and_in_range(cnv):
     assert counts.min() > 20  # roughly uniform over the six sizes
 
 
+def test_plan_of_the_256_cavity_workload(cnv):
+    """The decomposition the batch picks, planned on the host for a GB300 (152 blocks of 231424
+    bytes of shared memory): 384^2 and 256^2 cavities as 3-strip groups (the cost model's choice;
+    3 and 2 strips are the smallest that fit), the rest one block each, and an estimated step time
+    close to the balanced load."""
+    specs = cnv.batch_specs(256, seed=0)
+    groups, us = cnv.batch_plan(specs)
+    by_n = {}
+    for sp, g in zip(specs, groups):
+        by_n.setdefault(sp["n"], set()).add(g)
+    assert by_n == {64: {1}, 96: {1}, 128: {1}, 192: {1}, 256: {3}, 384: {3}}
+    assert 30e3 < us < 36e3, us  # measured on a GB300: 33.5 ms per step
+
+
+def test_plan_balances_a_few_large_cavities_and_rejects_bad_input(cnv):
+    # three cavities on 152 blocks: more strips than needed shorten the step
+    groups, us = cnv.batch_plan([dict(n=384, Re=1500.0, lid=1.2), dict(n=256, Re=300.0, lid=0.7),
+                                 dict(n=192, Re=900.0, lid=1.0)])
+    assert groups[0] > 3 and groups[1] >= 2 and groups[2] == 1, groups
+    one, us1 = cnv.batch_plan([dict(n=384, Re=1500.0, lid=1.2)], blocks=3)
+    assert one == [3] and us1 > us  # three blocks: the smallest count that fits, and slower
+    for bad in (dict(blocks=0), dict(smem_bytes=0)):
+        with pytest.raises(cnv.CnvError):
+            cnv.batch_plan(SPECS, **bad)
+    with pytest.raises(cnv.CnvError):
+        cnv.batch_plan([dict(n=384, Re=1.0, lid=1.0)], blocks=2)  # needs 3 blocks
+
+
 def _stable_dt(n, re, lid):
     h = 1.0 / n
     return 0.2 * min(h * h * re / 4, h / abs(lid))
