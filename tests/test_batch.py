@@ -187,6 +187,26 @@ def test_tuned_groups_on_large_cavities_equal_single_runs(cnv):
 
 
 @pytest.mark.gpu
+def test_default_strip_counts_equal_single_cavity_runs(cnv):
+    """The cost model's default decomposition of a few large cavities uses more strips than
+    shared memory needs (6 for 384^2 on a GB300, not a power of two); every cavity still equals
+    its single-cavity run."""
+    specs = [dict(n=384, Re=1500.0, lid=1.2), dict(n=256, Re=300.0, lid=0.7), dict(n=192, Re=900.0, lid=1.0)]
+    base = cnv.default_config(mixed_rtol=1e-10)
+    nsteps = 2
+    with cnv.Batch(base, specs) as bt:
+        groups = bt.groups()
+        rc, last = bt.step(nsteps)
+        fields = [bt.get_fields(k) for k in range(len(specs))]
+    assert rc == 0 and groups == cnv.batch_plan(specs)[0] and groups[0] == 6, groups
+    for k, sp in enumerate(specs):
+        steps, single = _single_mixed(cnv, sp, nsteps)
+        assert last[k]["iters"] == steps[-1]["iters"], k
+        for name, a, b in zip("w u v psi".split(), fields[k], single):
+            assert np.max(np.abs(a - b)) <= SAME_SCHEME_TOL * np.max(np.abs(b)), (k, name)
+
+
+@pytest.mark.gpu
 def test_large_cavities_on_their_smallest_strips(cnv):
     specs = [dict(n=384, Re=1500.0, lid=1.2), dict(n=256, Re=300.0, lid=0.7), dict(n=192, Re=900.0, lid=1.0)]
     base = cnv.default_config(mixed_rtol=1e-10)
