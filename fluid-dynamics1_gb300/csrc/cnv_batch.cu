@@ -810,15 +810,21 @@ void assign_groups(std::vector<CavityDesc>& desc, int smem_bytes, int split, int
     }
 }
 
-// Group sizes chosen by the cost model: every distinct cavity size whose correction needs row
-// strips gets a group from the smallest that fits to three more (strips at least 2 halos high,
-// at most `blocks`), the sizes tried jointly (the three largest such sizes; smaller ones keep the
-// smallest group), and the combination with the smallest estimated makespan is returned as
-// (n, group) pairs.
+// Smallest cavity that fits one block and that the cost model may still split: the model leaves
+// out the group barriers (about 4n/S + 20 per step), which only large cavities amortise.
+constexpr int kMinSplitN = 128;
+
+// Group sizes chosen by the cost model: each of the three largest distinct cavity sizes that
+// needs row strips, or fits one block and has at least kMinSplitN points, gets a group from the
+// smallest that fits to three more (strips at least 2 halos high, at most `blocks`), the sizes
+// tried jointly (smaller ones keep the smallest group), and the combination with the smallest
+// estimated makespan is returned as (n, group) pairs. A size that fits one block is so split when
+// that shortens the schedule (a few large cavities on many blocks).
 std::vector<std::pair<int, int>> model_groups(const std::vector<CavityDesc>& in, int smem_bytes, int blocks) {
     std::vector<int> sizes;
     for (const auto& d : in)
-        if (min_group(d.n, smem_bytes) >= 2 && std::find(sizes.begin(), sizes.end(), d.n) == sizes.end())
+        if ((min_group(d.n, smem_bytes) >= 2 || (min_group(d.n, smem_bytes) == 1 && d.n >= kMinSplitN)) &&
+            std::find(sizes.begin(), sizes.end(), d.n) == sizes.end())
             sizes.push_back(d.n);
     std::sort(sizes.rbegin(), sizes.rend());
     if (sizes.size() > 3) sizes.resize(3);
