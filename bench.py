@@ -364,6 +364,7 @@ def form_batched(cnvpy, local, steps, count=256, seed=0):
                                                                            "blocks_per_sm": per_sm},
                       "blocks_per_cavity": {str(n): groups[sample[i]] for i, n in
                                             enumerate(sorted({s["n"] for s in specs}))},
+                      "cost_model_ms_per_step": round(cnvpy.batch_plan(specs)[1] / 1e3, 3),
                       "max_relative_residual": max(x["err"] for x in last)}
     f_cells, f_ms, errs = 0, 0.0, {}
     for k in sample:
