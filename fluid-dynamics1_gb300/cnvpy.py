@@ -42,7 +42,7 @@ class Config(C.Structure):
         ("init_sigma", C.c_double), ("init_smooth_passes", C.c_int), ("device", C.c_int),
         ("solver_blocks", C.c_int), ("mixed_inner_sweeps", C.c_int), ("mixed_max_outer", C.c_int),
         ("sor_blocking", C.c_int), ("mixed_warm_start", C.c_int), ("solver_timeout_ms", C.c_int),
-        ("test_stall_block", C.c_int), ("reserved", C.c_int * 1),
+        ("test_stall_block", C.c_int), ("test_guard_cells", C.c_int),
     ]
 
 

@@ -91,6 +91,15 @@ void noise_field(int n, unsigned long long seed, double sigma, int passes, doubl
 
 void cnv::set_last_error(const char* msg) { g_last_error = msg; }
 
+// A device buffer allocated with guard regions (test_guard_cells): base is what cudaMalloc
+// returned, the buffer starts kGuardBytes later.
+constexpr size_t kGuardBytes = 4096;
+struct GuardedBuf {
+    char* base;
+    size_t bytes;
+    const char* name;
+};
+
 struct cnv_state {
     cnv_config cfg;
     int n = 0;
@@ -109,6 +118,7 @@ struct cnv_state {
     double* rhs[2] = {nullptr, nullptr};
     double* scratch = nullptr;   // 2*n*n: right-hand side and result of standalone Poisson solves
     double* stage = nullptr;     // 3*n*n: host fields uploaded by cnv_set_fields, checked on the device
+    std::vector<GuardedBuf> guarded;  // buffers with guard regions (test_guard_cells)
     void* sync = nullptr;        // Poisson solver synchronisation state
     // mixed-precision form (CNV_PREC_MIXED)
     bool mixed = false;
@@ -152,6 +162,56 @@ struct cnv_state {
 
 namespace {
 
+// cudaMalloc for a field or work buffer. With test_guard_cells, kGuardBytes of 0xFF bytes (a NaN
+// in every lane width) sit before and after the buffer, and check_guards verifies them after each
+// step and Poisson call: a kernel that writes past either end of its buffer is reported by name.
+// 4096 bytes keep the buffer's 256-byte alignment.
+cudaError_t buf_alloc(cnv_state* s, void** p, size_t bytes, const char* name) {
+    if (!s->cfg.test_guard_cells) return cudaMalloc(p, bytes);
+    char* base = nullptr;
+    cudaError_t e = cudaMalloc(&base, bytes + 2 * kGuardBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaMemset(base, 0xFF, kGuardBytes);
+    if (e == cudaSuccess) e = cudaMemset(base + kGuardBytes + bytes, 0xFF, kGuardBytes);
+    if (e != cudaSuccess) {
+        cudaFree(base);
+        return e;
+    }
+    s->guarded.push_back(GuardedBuf{base, bytes, name});
+    *p = base + kGuardBytes;
+    return cudaSuccess;
+}
+
+void buf_free(cnv_state* s, void* p) {
+    if (!p) return;
+    for (auto& g : s->guarded)
+        if (g.base && g.base + kGuardBytes == p) {
+            cudaFree(g.base);
+            g.base = nullptr;
+            return;
+        }
+    cudaFree(p);
+}
+
+// CNV_OK, or CNV_CUDA_ERROR naming the first buffer whose guard bytes changed.
+int check_guards(cnv_state* s) {
+    if (s->guarded.empty()) return CNV_OK;
+    CNV_CUDA(cudaStreamSynchronize(s->stream));
+    std::vector<unsigned char> h(kGuardBytes);
+    for (const auto& g : s->guarded) {
+        if (!g.base) continue;
+        for (int after = 0; after < 2; ++after) {
+            CNV_CUDA(cudaMemcpy(h.data(), after ? g.base + kGuardBytes + g.bytes : g.base, kGuardBytes,
+                                cudaMemcpyDeviceToHost));
+            for (size_t k = 0; k < kGuardBytes; ++k)
+                if (h[k] != 0xFF)
+                    return fail(CNV_CUDA_ERROR, "guard bytes %s %s changed (byte %zu of %zu)", after ? "after" : "before",
+                                g.name, k, kGuardBytes);
+        }
+    }
+    return CNV_OK;
+}
+
 void free_state(cnv_state* s) {
     if (!s) return;
     if (s->device >= 0) cudaSetDevice(s->device);
@@ -160,18 +220,16 @@ void free_state(cnv_state* s) {
             if (g) cudaGraphExecDestroy(g);
     double* bufs[] = {s->w[0], s->w[1], s->u, s->v, s->psi, s->sor[0], s->sor[1], s->alt[0],
                       s->alt[1], s->rhs[0], s->rhs[1], s->scratch, s->stage, s->cont_partials};
-    for (double* b : bufs)
-        if (b) cudaFree(b);
-    for (float* b : {s->rq, s->eg})
-        if (b) cudaFree(b);
+    for (double* b : bufs) buf_free(s, b);
+    for (float* b : {s->rq, s->eg}) buf_free(s, b);
     if (s->msync) cudaFree(s->msync);
-    if (s->tb_snap) cudaFree(s->tb_snap);
+    buf_free(s, s->tb_snap);
     if (s->tb_sync) cudaFree(s->tb_sync);
     if (s->direct) dst_plan_destroy(&s->dst);
-    if (s->flag) cudaFree(s->flag);
+    buf_free(s, s->flag);
     if (s->sync) cudaFree(s->sync);
-    if (s->bands) cudaFree(s->bands);
-    if (s->ctrl) cudaFree(s->ctrl);
+    buf_free(s, s->bands);
+    buf_free(s, s->ctrl);
     if (s->records) cudaFree(s->records);
     for (cudaEvent_t ev : {s->ev0, s->ev1, s->evp0, s->evp1})
         if (ev) cudaEventDestroy(ev);
@@ -189,6 +247,8 @@ int validate(const cnv_config* c) {
     if (c->poisson_type < 1 || c->poisson_type > 4)
         return fail(CNV_BAD_ARG, "Error - invalid option for Poisson solver (%d)", c->poisson_type);
     if (c->test_stall_block < 0) return fail(CNV_BAD_ARG, "test_stall_block must be >= 0");
+    if (c->test_guard_cells < 0 || c->test_guard_cells > 2)
+        return fail(CNV_BAD_ARG, "test_guard_cells must be 0, 1 or 2, got %d", c->test_guard_cells);
     if (c->sor_blocking != 0 && c->sor_blocking != 1 && c->sor_blocking != 2 && c->sor_blocking != 4)
         return fail(CNV_BAD_ARG, "sor_blocking must be 0 (auto), 1, 2 or 4 sweeps per exchange, got %d",
                     c->sor_blocking);
@@ -454,7 +514,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     const size_t split = (size_t)n * s->pitch;
 #define ALLOC(ptr, count)                                                     \
     do {                                                                      \
-        cudaError_t e_ = cudaMalloc(&(ptr), sizeof(*(ptr)) * (count));        \
+        cudaError_t e_ = buf_alloc(s, reinterpret_cast<void**>(&(ptr)), sizeof(*(ptr)) * (count), #ptr); \
         if (e_ != cudaSuccess) {                                              \
             free_state(s);                                                    \
             return fail(CNV_CUDA_ERROR, "cudaMalloc: %s", cudaGetErrorString(e_)); \
@@ -560,7 +620,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
             s->tb = true;
             s->tb_g_smem = tb_smem_bytes(n, s->tb_gx, s->tb_gy, want_sweeps, true) + 2048 <= optin;
             const size_t snap = tb_snapshot_doubles(n, s->pitch);
-            if (cudaMalloc(&s->tb_snap, snap * sizeof(double)) != cudaSuccess ||
+            if (buf_alloc(s, reinterpret_cast<void**>(&s->tb_snap), snap * sizeof(double), "s->tb_snap") != cudaSuccess ||
                 cudaMalloc(&s->tb_sync, tb_sync_bytes()) != cudaSuccess) {
                 free_state(s);
                 return fail(CNV_CUDA_ERROR, "cudaMalloc failed (tiled solver buffers)");
@@ -655,6 +715,12 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     }
     rc = ensure_records(s, 64);
     if (rc == CNV_OK) rc = upload_initial(s);
+    if (rc == CNV_OK && cfg->test_guard_cells == 2) {
+        // the checker's own test: one changed byte in the guard after u
+        for (const auto& g : s->guarded)
+            if (!strcmp(g.name, "s->u") && cudaMemset(g.base + kGuardBytes + g.bytes, 0, 1) != cudaSuccess)
+                rc = fail(CNV_CUDA_ERROR, "guard setup failed");
+    }
     if (rc != CNV_OK) {
         free_state(s);
         return rc;
@@ -785,6 +851,7 @@ int cnv_sync(cnv_state* s, cnv_step_info* info, int ninfo) {
     }
     if (info)
         for (int t = 0; t < std::min(ninfo, nsteps); ++t) std::memcpy(&info[t], &rec[t], sizeof(StepRecord));
+    if (rc == CNV_OK) rc = check_guards(s);
     return rc;
 }
 
@@ -841,7 +908,7 @@ int cnv_poisson_device(cnv_state* s, const double* f, double* psi_out, int* iter
     if (iters) *iters = h.iters;
     if (err) *err = h.err;
     if (h.status != CNV_OK) return fail(h.status, "Poisson solve status %d", h.status);
-    return CNV_OK;
+    return check_guards(s);
 }
 
 int cnv_poisson(cnv_state* s, const double* f, double* psi, int* iters, double* err) {

@@ -106,7 +106,11 @@ typedef struct cnv_config {
     int test_stall_block;    /* testing only: 1 + the index of a block of the FP64 SOR/GS exchange
                                 kernel that never raises its progress flags, so that its neighbours'
                                 bounded waits run out (the solve returns CNV_TIMEOUT); 0: off */
-    int reserved[1];
+    int test_guard_cells;    /* testing only: 1 puts 4 KB of 0xFF bytes (NaN in every lane width)
+                                before and after every field and work buffer and checks them after
+                                each step and Poisson call (CNV_CUDA_ERROR naming the buffer if a
+                                kernel wrote there); 2 also changes one guard byte after u at
+                                creation, so the first check must report it; 0: off */
 } cnv_config;
 
 /* Per-step record: the values the reference logs (src/poisson.c:275, src/main.c:407-408). */

@@ -103,7 +103,8 @@ def test_missing_config_file_keeps_defaults(cnv, tmp_path):
 
 
 @pytest.mark.parametrize("field,value", [("ny", 63), ("order", 3), ("poisson_type", 5), ("nx", 3),
-                                         ("precision", 9), ("dt", 0.0), ("u1", 1e6)])
+                                         ("precision", 9), ("dt", 0.0), ("u1", 1e6), ("test_guard_cells", 3),
+                                         ("test_stall_block", -1)])
 def test_create_rejects_bad_arguments_without_touching_the_gpu(cnv, field, value):
     cfg = cnv.default_config()
     setattr(cfg, field, value)
