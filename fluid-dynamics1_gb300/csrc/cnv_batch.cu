@@ -66,6 +66,7 @@ struct CavityDesc {
 
 // Group barrier and reductions of one cavity's group (zeroed before every launch).
 constexpr int kMaxGroup = 16;
+constexpr size_t kBatchGuardBytes = 4096;  // guard region size (test_guard_cells)
 struct GroupSync {
     unsigned int bar;
     unsigned int pad;
@@ -607,6 +608,9 @@ struct cnv_batch {
     FdBands* bands = nullptr;
     void* arena = nullptr;
     size_t arena_bytes = 0;
+    // test_guard_cells: byte offsets into the arena of the guard regions (kBatchGuardBytes of 0xFF
+    // before the first buffer and after every buffer) and what each follows
+    std::vector<std::pair<size_t, std::string>> guards;
     SchedEntry* sched = nullptr;   // job lists (device)
     int* sched_off = nullptr;      // per block offsets into sched (device)
     GroupSync* gsync = nullptr;    // per cavity (device)
@@ -634,6 +638,21 @@ namespace {
 int bfail(int status, const std::string& msg) {
     set_last_error(msg.c_str());
     return status;
+}
+
+// CNV_OK, or CNV_CUDA_ERROR naming the first guard region (test_guard_cells) whose bytes changed.
+int check_guards(cnv_batch* b) {
+    if (b->guards.empty()) return CNV_OK;
+    std::vector<unsigned char> h(kBatchGuardBytes);
+    for (const auto& g : b->guards) {
+        if (cudaMemcpy(h.data(), static_cast<char*>(b->arena) + g.first, kBatchGuardBytes, cudaMemcpyDeviceToHost) !=
+            cudaSuccess)
+            return bfail(CNV_CUDA_ERROR, "guard check: copy failed");
+        for (size_t k = 0; k < kBatchGuardBytes; ++k)
+            if (h[k] != 0xFF)
+                return bfail(CNV_CUDA_ERROR, "guard bytes " + g.second + " changed (byte " + std::to_string(k) + ")");
+    }
+    return CNV_OK;
 }
 
 #define BCUDA(call)                                                                                   \
@@ -886,6 +905,8 @@ int set_shape(cnv_batch* b, int threads, int per_sm) {
 
 int reset_fields(cnv_batch* b) {
     BCUDA(cudaMemsetAsync(b->arena, 0, b->arena_bytes, b->stream));
+    for (const auto& g : b->guards)
+        BCUDA(cudaMemsetAsync(static_cast<char*>(b->arena) + g.first, 0xFF, kBatchGuardBytes, b->stream));
     for (auto& d : b->host_desc) d.cur = 0;
     BCUDA(cudaMemcpyAsync(b->desc, b->host_desc.data(), sizeof(CavityDesc) * b->count, cudaMemcpyHostToDevice,
                           b->stream));
@@ -949,6 +970,8 @@ int cnv_batch_plan(int count, const cnv_cavity_spec* specs, int blocks, int smem
 int cnv_batch_create(const cnv_config* base, int count, const cnv_cavity_spec* specs, cnv_batch** out) {
     if (!base || !specs || !out || count < 1) return bfail(CNV_BAD_ARG, "null argument or empty batch");
     *out = nullptr;
+    if (base->test_guard_cells < 0 || base->test_guard_cells > 2)
+        return bfail(CNV_BAD_ARG, "test_guard_cells must be 0, 1 or 2");
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, base->device) != cudaSuccess || prop.major != 10 || prop.minor != 3)
         return bfail(CNV_NO_DEVICE, "no sm_103 device");
@@ -975,19 +998,26 @@ int cnv_batch_create(const cnv_config* base, int count, const cnv_cavity_spec* s
         return cleanup(CNV_CUDA_ERROR, "stream/event creation failed");
 
     // arena: per cavity w[2], u, v, psi_rm (n*n doubles each), psi/g split (2 x n*pitch doubles
-    // each), e/rq/ex1 split (2 x n*pitch floats each)
-    std::vector<size_t> offs(count);
-    size_t total = 0;
+    // each), e/rq/ex1 split (2 x n*pitch floats each), each 256-byte aligned; with
+    // test_guard_cells a guard region before the first and after every buffer
+    const size_t gap = base->test_guard_cells ? kBatchGuardBytes : 0;
     auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    auto cavity_bytes = [&](int n, int pitch) {
+        return 5 * (align((size_t)n * n * 8) + gap) + 4 * (align((size_t)n * pitch * 8) + gap) +
+               6 * (align((size_t)n * pitch * 4) + gap);
+    };
+    std::vector<size_t> offs(count);
+    size_t total = gap;
     b->host_desc.resize(count);
     for (int k = 0; k < count; ++k) {
         const int n = specs[k].n;
         const int pitch = ((n + 1) / 2 + 31) / 32 * 32;
         offs[k] = total;
-        total += align(5 * (size_t)n * n * 8) + align(4 * (size_t)n * pitch * 8) + align(6 * (size_t)n * pitch * 4);
+        total += cavity_bytes(n, pitch);
         b->cells += (long long)n * n;
     }
     b->arena_bytes = total;
+    if (gap) b->guards.emplace_back(0, "before cavity 0");
     if (cudaMalloc(&b->arena, total) != cudaSuccess) return cleanup(CNV_CUDA_ERROR, "arena allocation failed");
     if (cudaMalloc(&b->desc, sizeof(CavityDesc) * count) != cudaSuccess ||
         cudaMalloc(&b->bands, sizeof(FdBands) * count) != cudaSuccess ||
@@ -1027,25 +1057,30 @@ int cnv_batch_create(const cnv_config* base, int count, const cnv_cavity_spec* s
         const int per_epoch = mixed_sweeps_per_exchange();
         d.inner = std::max(1, (want + per_epoch - 1) / per_epoch) * per_epoch;
         d.bands = b->bands + k;
-        char* p = static_cast<char*>(b->arena) + offs[k];
-        double* f64 = reinterpret_cast<double*>(p);
-        d.w[0] = f64;
-        d.w[1] = f64 + (size_t)n * n;
-        d.u = f64 + 2 * (size_t)n * n;
-        d.v = f64 + 3 * (size_t)n * n;
-        d.psi_rm = f64 + 4 * (size_t)n * n;
-        double* split = reinterpret_cast<double*>(p + align(5 * (size_t)n * n * 8));
-        d.psi[0] = split;
-        d.psi[1] = split + (size_t)n * pitch;
-        d.g[0] = split + 2 * (size_t)n * pitch;
-        d.g[1] = split + 3 * (size_t)n * pitch;
-        float* f32 = reinterpret_cast<float*>(p + align(5 * (size_t)n * n * 8) + align(4 * (size_t)n * pitch * 8));
-        d.e[0] = f32;
-        d.e[1] = f32 + (size_t)n * pitch;
-        d.rq[0] = f32 + 2 * (size_t)n * pitch;
-        d.rq[1] = f32 + 3 * (size_t)n * pitch;
-        d.ex1[0] = f32 + 4 * (size_t)n * pitch;
-        d.ex1[1] = f32 + 5 * (size_t)n * pitch;
+        size_t cur = offs[k];
+        auto take = [&](size_t bytes, const char* name) {
+            char* q = static_cast<char*>(b->arena) + cur;
+            cur += align(bytes);
+            if (gap) b->guards.emplace_back(cur, "after cavity " + std::to_string(k) + "'s " + name);
+            cur += gap;
+            return q;
+        };
+        const size_t f64b = (size_t)n * n * 8, sp64 = (size_t)n * pitch * 8, sp32 = (size_t)n * pitch * 4;
+        d.w[0] = reinterpret_cast<double*>(take(f64b, "w[0]"));
+        d.w[1] = reinterpret_cast<double*>(take(f64b, "w[1]"));
+        d.u = reinterpret_cast<double*>(take(f64b, "u"));
+        d.v = reinterpret_cast<double*>(take(f64b, "v"));
+        d.psi_rm = reinterpret_cast<double*>(take(f64b, "psi"));
+        d.psi[0] = reinterpret_cast<double*>(take(sp64, "split psi[0]"));
+        d.psi[1] = reinterpret_cast<double*>(take(sp64, "split psi[1]"));
+        d.g[0] = reinterpret_cast<double*>(take(sp64, "g[0]"));
+        d.g[1] = reinterpret_cast<double*>(take(sp64, "g[1]"));
+        d.e[0] = reinterpret_cast<float*>(take(sp32, "e[0]"));
+        d.e[1] = reinterpret_cast<float*>(take(sp32, "e[1]"));
+        d.rq[0] = reinterpret_cast<float*>(take(sp32, "rq[0]"));
+        d.rq[1] = reinterpret_cast<float*>(take(sp32, "rq[1]"));
+        d.ex1[0] = reinterpret_cast<float*>(take(sp32, "ex1[0]"));
+        d.ex1[1] = reinterpret_cast<float*>(take(sp32, "ex1[1]"));
         d.group = 1;
     }
     if (cudaMemcpy(b->bands, hb.data(), sizeof(FdBands) * count, cudaMemcpyHostToDevice) != cudaSuccess)
@@ -1056,6 +1091,13 @@ int cnv_batch_create(const cnv_config* base, int count, const cnv_cavity_spec* s
     if (rc == CNV_OK) {
         model_groups(b);
         rc = set_shape(b, 1024, 1);
+    }
+    if (rc == CNV_OK && base->test_guard_cells == 2) {
+        // the checker's own test: one changed byte in the guard after cavity 0's u
+        for (const auto& g : b->guards)
+            if (g.second == "after cavity 0's u" &&
+                cudaMemset(static_cast<char*>(b->arena) + g.first, 0, 1) != cudaSuccess)
+                rc = bfail(CNV_CUDA_ERROR, "guard setup failed");
     }
     if (rc != CNV_OK) {
         cnv_batch_destroy(b);
@@ -1147,6 +1189,8 @@ int cnv_batch_step(cnv_batch* b, int nsteps, cnv_step_info* last) {
     if (!b || nsteps < 0) return bfail(CNV_BAD_ARG, "bad batch or step count");
     BCUDA(cudaSetDevice(b->device));
     int rc = run(b, nsteps);
+    if (rc != CNV_OK) return rc;
+    rc = check_guards(b);
     if (rc != CNV_OK) return rc;
     int aborted = 0;
     BCUDA(cudaMemcpy(&aborted, b->abort, sizeof(int), cudaMemcpyDeviceToHost));

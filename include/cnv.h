@@ -110,7 +110,9 @@ typedef struct cnv_config {
                                 before and after every field and work buffer and checks them after
                                 each step and Poisson call (CNV_CUDA_ERROR naming the buffer if a
                                 kernel wrote there); 2 also changes one guard byte after u at
-                                creation, so the first check must report it; 0: off */
+                                creation, so the first check must report it; 0: off. Batches
+                                (cnv_batch_create's base) put a guard after every buffer of every
+                                cavity in their arena and check after each cnv_batch_step */
 } cnv_config;
 
 /* Per-step record: the values the reference logs (src/poisson.c:275, src/main.c:407-408). */

@@ -59,3 +59,40 @@ def test_guard_check_reports_a_changed_byte(cnv):
         rc, _ = cav.step(1, raise_on_error=False)
         assert rc == cnv.CNV_CUDA_ERROR
         assert "after s->u" in cnv.last_error()
+
+
+# ------------------------------------------------------------------------------ batched form
+BATCH = [dict(n=384, Re=1500.0, lid=1.2), dict(n=256, Re=300.0, lid=0.7), dict(n=96, Re=900.0, lid=1.0),
+         dict(n=40, Re=1200.0, lid=0.8), dict(n=33, Re=150.0, lid=1.4)]
+
+
+def run_batch(cnv, guards, split):
+    base = cnv.default_config(mixed_rtol=1e-10, test_guard_cells=guards)
+    with cnv.Batch(base, BATCH) as bt:
+        if split:
+            bt.split(4, 1)
+        groups = bt.groups()
+        rc, _ = bt.step(2)
+        assert rc == cnv.CNV_OK, cnv.last_error()
+        return groups, [bt.get_fields(k) for k in range(len(BATCH))]
+
+
+@pytest.mark.parametrize("split", [False, True], ids=["model-strips", "4x-strips"])
+def test_no_batch_kernel_writes_outside_its_buffers(cnv, split):
+    """Every buffer of every cavity in the batch arena is followed by a guard region: one-block
+    cavities, row-strip groups of the cost model's sizes, and 2- to 4-strip groups of small
+    cavities leave all of them intact, with the same fields as the unguarded batch."""
+    g0, plain = run_batch(cnv, 0, split)
+    g1, guarded = run_batch(cnv, 1, split)
+    assert g0 == g1 and max(g1) > 1
+    for fa, fb in zip(plain, guarded):
+        for a, b in zip(fa, fb):
+            assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def test_batch_guard_check_reports_a_changed_byte(cnv):
+    base = cnv.default_config(mixed_rtol=1e-10, test_guard_cells=2)
+    with cnv.Batch(base, BATCH[2:]) as bt:
+        rc, _ = bt.step(1, raise_on_error=False)
+        assert rc == cnv.CNV_CUDA_ERROR
+        assert "after cavity 0's u" in cnv.last_error()
