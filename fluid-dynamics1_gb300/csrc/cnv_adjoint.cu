@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "cnv_dst.h"
+#include "cnv_guard.h"
 #include "cnv_kernels.h"
 #include "cnv_stencil.cuh"
 
@@ -185,6 +186,7 @@ struct cnv_adjoint {
     double lid = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     double fwd_ms = 0, bwd_ms = 0;
+    GuardSet guards;  // guard regions around the field buffers (test_guard_cells)
 };
 
 namespace {
@@ -201,14 +203,19 @@ int afail(int status, const std::string& msg) {
             return afail(CNV_CUDA_ERROR, std::string(#call) + " failed: " + cudaGetErrorString(e_));   \
     } while (0)
 
+// CNV_OK, or CNV_CUDA_ERROR naming the first buffer whose guard bytes changed (test_guard_cells).
+int check_guards(cnv_adjoint* a) {
+    std::string what;
+    return a->guards.check(&what) ? CNV_OK : afail(CNV_CUDA_ERROR, what);
+}
+
 void free_adjoint(cnv_adjoint* a) {
     if (!a) return;
     cudaSetDevice(a->device);
     dst_plan_destroy(&a->dst);
     double* bufs[] = {a->sor[0], a->sor[1], a->psi, a->u0, a->v0, a->w[0], a->w[1], a->u, a->v, a->ck, a->seg,
                       a->lw, a->lu, a->lv, a->lpsi, a->mu, a->lwb, a->lub, a->lvb, a->lid_row, a->stage};
-    for (double* b : bufs)
-        if (b) cudaFree(b);
+    for (double* b : bufs) a->guards.release(b);
     if (a->bands) cudaFree(a->bands);
     if (a->ctrl) cudaFree(a->ctrl);
     for (cudaEvent_t e : a->ev)
@@ -223,12 +230,12 @@ double* slot_w(double* base, size_t nn, size_t k) { return base + 3 * nn * k; }
 double* slot_u(double* base, size_t nn, size_t k) { return base + 3 * nn * k + nn; }
 double* slot_v(double* base, size_t nn, size_t k) { return base + 3 * nn * k + 2 * nn; }
 
-int ensure_slots(double** buf, size_t* have, size_t want, size_t nn) {
+int ensure_slots(GuardSet& guards, double** buf, size_t* have, size_t want, size_t nn, const char* name) {
     if (want <= *have) return CNV_OK;
-    if (*buf) ACUDA(cudaFree(*buf));
+    guards.release(*buf);
     *buf = nullptr;
     *have = 0;
-    ACUDA(cudaMalloc(buf, want * 3 * nn * sizeof(double)));
+    ACUDA(guards.alloc(reinterpret_cast<void**>(buf), want * 3 * nn * sizeof(double), name));
     *have = want;
     return CNV_OK;
 }
@@ -275,7 +282,7 @@ int run_forward(cnv_adjoint* a, const double* w0_dev, double lid, int nsteps, bo
     a->steps = -1;
     if (checkpoints) {
         const size_t want = (size_t)(nsteps + a->every - 1) / a->every;
-        int rc = ensure_slots(&a->ck, &a->ck_slots, std::max<size_t>(want, 1), nn);
+        int rc = ensure_slots(a->guards, &a->ck, &a->ck_slots, std::max<size_t>(want, 1), nn, "checkpoints");
         if (rc != CNV_OK) return rc;
     }
     ACUDA(cudaMemcpyAsync(a->w[0], w0_dev, nn * 8, cudaMemcpyDeviceToDevice, a->stream));
@@ -304,7 +311,7 @@ int run_backward(cnv_adjoint* a, const double* gT_dev, double* gw0_dev, double* 
     const int T = a->steps;
     const size_t nn = nn_of(a);
     const int n = a->n;
-    int rc = ensure_slots(&a->seg, &a->seg_slots, (size_t)a->every + 1, nn);
+    int rc = ensure_slots(a->guards, &a->seg, &a->seg_slots, (size_t)a->every + 1, nn, "segment states");
     if (rc != CNV_OK) return rc;
     ACUDA(cudaEventRecord(a->ev[2], a->stream));
     ACUDA(cudaMemcpyAsync(a->lw, gT_dev, nn * 8, cudaMemcpyDeviceToDevice, a->stream));
@@ -392,12 +399,15 @@ int cnv_adjoint_create(const cnv_config* cfg, int checkpoint_every, cnv_adjoint*
     if (!(cfg->Re > 0) || !(cfg->dt > 0) || cfg->Lx <= 0 || cfg->Ly <= 0)
         return afail(CNV_BAD_ARG, "invalid Re/dt/Lx/Ly");
     if (checkpoint_every < 1) return afail(CNV_BAD_ARG, "checkpoint_every must be >= 1");
+    if (cfg->test_guard_cells < 0 || cfg->test_guard_cells > 2)
+        return afail(CNV_BAD_ARG, "test_guard_cells must be 0, 1 or 2");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= cfg->device)
         return afail(CNV_NO_DEVICE, "no CUDA device " + std::to_string(cfg->device));
     ACUDA(cudaSetDevice(cfg->device));
     cnv_adjoint* a = new cnv_adjoint();
     a->cfg = *cfg;
+    a->guards.on = cfg->test_guard_cells != 0;
     a->device = cfg->device;
     a->n = cfg->nx;
     a->every = checkpoint_every;
@@ -417,15 +427,21 @@ int cnv_adjoint_create(const cnv_config* cfg, int checkpoint_every, cnv_adjoint*
         if (cudaEventCreate(&e) != cudaSuccess) return bad("event");
     double** fields[] = {&a->psi, &a->u0, &a->v0, &a->w[0], &a->w[1], &a->u, &a->v, &a->lw, &a->lu,
                          &a->lv, &a->lpsi, &a->mu, &a->lwb, &a->lub, &a->lvb, &a->stage};
-    for (double** f : fields) {
-        if (cudaMalloc(f, nn * 8) != cudaSuccess) return bad("cudaMalloc");
-        if (cudaMemset(*f, 0, nn * 8) != cudaSuccess) return bad("cudaMemset");
+    const char* names[] = {"psi", "u0", "v0", "w[0]", "w[1]", "u", "v", "lw", "lu",
+                           "lv", "lpsi", "mu", "lwb", "lub", "lvb", "stage"};
+    for (int k = 0; k < 16; ++k) {
+        if (a->guards.alloc(reinterpret_cast<void**>(fields[k]), nn * 8, names[k]) != cudaSuccess)
+            return bad("cudaMalloc");
+        if (cudaMemset(*fields[k], 0, nn * 8) != cudaSuccess) return bad("cudaMemset");
     }
-    for (auto& p : a->sor) {
-        if (cudaMalloc(&p, split * 8) != cudaSuccess) return bad("cudaMalloc");
-        if (cudaMemset(p, 0, split * 8) != cudaSuccess) return bad("cudaMemset");
+    const char* sor_names[] = {"split psi[0]", "split psi[1]"};
+    for (int c = 0; c < 2; ++c) {
+        if (a->guards.alloc(reinterpret_cast<void**>(&a->sor[c]), split * 8, sor_names[c]) != cudaSuccess)
+            return bad("cudaMalloc");
+        if (cudaMemset(a->sor[c], 0, split * 8) != cudaSuccess) return bad("cudaMemset");
     }
-    if (cudaMalloc(&a->lid_row, n * 8) != cudaSuccess) return bad("cudaMalloc");
+    if (a->guards.alloc(reinterpret_cast<void**>(&a->lid_row), n * 8, "lid_row") != cudaSuccess)
+        return bad("cudaMalloc");
     if (cudaMalloc(&a->bands, sizeof(FdBands)) != cudaSuccess || cudaMalloc(&a->ctrl, sizeof(Ctrl)) != cudaSuccess)
         return bad("cudaMalloc");
     if (cudaMemset(a->ctrl, 0, sizeof(Ctrl)) != cudaSuccess) return bad("cudaMemset");
@@ -446,6 +462,7 @@ int cnv_adjoint_create(const cnv_config* cfg, int checkpoint_every, cnv_adjoint*
     if (cudaMemcpy(a->u0, hu.data(), nn * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(a->v0, hv.data(), nn * 8, cudaMemcpyHostToDevice) != cudaSuccess)
         return bad("initial velocity upload");
+    if (cfg->test_guard_cells == 2 && a->guards.plant("u") != cudaSuccess) return bad("guard setup");
     *out = a;
     return CNV_OK;
 }
@@ -463,14 +480,15 @@ int cnv_adjoint_forward_device(cnv_adjoint* a, const double* w0, double lid, int
     float ms = 0;
     cudaEventElapsedTime(&ms, a->ev[0], a->ev[1]);
     a->fwd_ms = ms;
-    return CNV_OK;
+    return check_guards(a);
 }
 
 int cnv_adjoint_backward_device(cnv_adjoint* a, const double* g_final, double* g_w0, double* g_lid) {
     if (!a || !g_final || !g_w0) return afail(CNV_BAD_ARG, "null argument");
     if (a->steps < 1) return afail(CNV_BAD_ARG, "no forward run to differentiate");
     ACUDA(cudaSetDevice(a->device));
-    return run_backward(a, g_final, g_w0, g_lid);
+    const int rc = run_backward(a, g_final, g_w0, g_lid);
+    return rc == CNV_OK ? check_guards(a) : rc;
 }
 
 int cnv_adjoint_forward(cnv_adjoint* a, const double* w0, double lid, int nsteps, double* w_final) {
@@ -488,7 +506,7 @@ int cnv_adjoint_forward(cnv_adjoint* a, const double* w0, double lid, int nsteps
     a->fwd_ms = ms;
     if (w_final) std::memcpy(w_final, h.data(), nn * 8);
     if (!finite_all(h)) return afail(CNV_NONFINITE, "final vorticity holds NaN or Inf");
-    return CNV_OK;
+    return check_guards(a);
 }
 
 int cnv_adjoint_backward(cnv_adjoint* a, const double* g_final, double* g_w0, double* g_lid) {
@@ -501,7 +519,7 @@ int cnv_adjoint_backward(cnv_adjoint* a, const double* g_final, double* g_w0, do
     if (rc != CNV_OK) return rc;
     ACUDA(cudaMemcpyAsync(g_w0, a->lw, nn * 8, cudaMemcpyDeviceToHost, a->stream));
     ACUDA(cudaStreamSynchronize(a->stream));
-    return CNV_OK;
+    return check_guards(a);
 }
 
 int cnv_adjoint_enstrophy_gradient(cnv_adjoint* a, const double* w0, double lid, int nsteps, double* J,

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "cnv_dst.h"
+#include "cnv_guard.h"
 #include "cnv_kernels.h"
 
 using namespace cnv;
@@ -91,15 +92,6 @@ void noise_field(int n, unsigned long long seed, double sigma, int passes, doubl
 
 void cnv::set_last_error(const char* msg) { g_last_error = msg; }
 
-// A device buffer allocated with guard regions (test_guard_cells): base is what cudaMalloc
-// returned, the buffer starts kGuardBytes later.
-constexpr size_t kGuardBytes = 4096;
-struct GuardedBuf {
-    char* base;
-    size_t bytes;
-    const char* name;
-};
-
 struct cnv_state {
     cnv_config cfg;
     int n = 0;
@@ -118,7 +110,7 @@ struct cnv_state {
     double* rhs[2] = {nullptr, nullptr};
     double* scratch = nullptr;   // 2*n*n: right-hand side and result of standalone Poisson solves
     double* stage = nullptr;     // 3*n*n: host fields uploaded by cnv_set_fields, checked on the device
-    std::vector<GuardedBuf> guarded;  // buffers with guard regions (test_guard_cells)
+    GuardSet guards;             // guard regions around the buffers (test_guard_cells)
     void* sync = nullptr;        // Poisson solver synchronisation state
     // mixed-precision form (CNV_PREC_MIXED)
     bool mixed = false;
@@ -162,54 +154,16 @@ struct cnv_state {
 
 namespace {
 
-// cudaMalloc for a field or work buffer. With test_guard_cells, kGuardBytes of 0xFF bytes (a NaN
-// in every lane width) sit before and after the buffer, and check_guards verifies them after each
-// step and Poisson call: a kernel that writes past either end of its buffer is reported by name.
-// 4096 bytes keep the buffer's 256-byte alignment.
-cudaError_t buf_alloc(cnv_state* s, void** p, size_t bytes, const char* name) {
-    if (!s->cfg.test_guard_cells) return cudaMalloc(p, bytes);
-    char* base = nullptr;
-    cudaError_t e = cudaMalloc(&base, bytes + 2 * kGuardBytes);
-    if (e != cudaSuccess) return e;
-    e = cudaMemset(base, 0xFF, kGuardBytes);
-    if (e == cudaSuccess) e = cudaMemset(base + kGuardBytes + bytes, 0xFF, kGuardBytes);
-    if (e != cudaSuccess) {
-        cudaFree(base);
-        return e;
-    }
-    s->guarded.push_back(GuardedBuf{base, bytes, name});
-    *p = base + kGuardBytes;
-    return cudaSuccess;
-}
+// cudaMalloc for a field or work buffer, with guard regions when test_guard_cells is on.
+cudaError_t buf_alloc(cnv_state* s, void** p, size_t bytes, const char* name) { return s->guards.alloc(p, bytes, name); }
 
-void buf_free(cnv_state* s, void* p) {
-    if (!p) return;
-    for (auto& g : s->guarded)
-        if (g.base && g.base + kGuardBytes == p) {
-            cudaFree(g.base);
-            g.base = nullptr;
-            return;
-        }
-    cudaFree(p);
-}
+void buf_free(cnv_state* s, void* p) { s->guards.release(p); }
 
-// CNV_OK, or CNV_CUDA_ERROR naming the first buffer whose guard bytes changed.
+// CNV_OK, or CNV_CUDA_ERROR naming the first buffer whose guard bytes changed (test_guard_cells).
 int check_guards(cnv_state* s) {
-    if (s->guarded.empty()) return CNV_OK;
-    CNV_CUDA(cudaStreamSynchronize(s->stream));
-    std::vector<unsigned char> h(kGuardBytes);
-    for (const auto& g : s->guarded) {
-        if (!g.base) continue;
-        for (int after = 0; after < 2; ++after) {
-            CNV_CUDA(cudaMemcpy(h.data(), after ? g.base + kGuardBytes + g.bytes : g.base, kGuardBytes,
-                                cudaMemcpyDeviceToHost));
-            for (size_t k = 0; k < kGuardBytes; ++k)
-                if (h[k] != 0xFF)
-                    return fail(CNV_CUDA_ERROR, "guard bytes %s %s changed (byte %zu of %zu)", after ? "after" : "before",
-                                g.name, k, kGuardBytes);
-        }
-    }
-    return CNV_OK;
+    std::string what;
+    if (s->guards.check(&what)) return CNV_OK;
+    return fail(CNV_CUDA_ERROR, "%s", what.c_str());
 }
 
 void free_state(cnv_state* s) {
@@ -502,6 +456,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
 
     cnv_state* s = new cnv_state();
     s->cfg = *cfg;
+    s->guards.on = cfg->test_guard_cells != 0;
     s->device = cfg->device;
     s->n = cfg->nx;
     s->sms = prop.multiProcessorCount;
@@ -715,12 +670,8 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     }
     rc = ensure_records(s, 64);
     if (rc == CNV_OK) rc = upload_initial(s);
-    if (rc == CNV_OK && cfg->test_guard_cells == 2) {
-        // the checker's own test: one changed byte in the guard after u
-        for (const auto& g : s->guarded)
-            if (!strcmp(g.name, "s->u") && cudaMemset(g.base + kGuardBytes + g.bytes, 0, 1) != cudaSuccess)
-                rc = fail(CNV_CUDA_ERROR, "guard setup failed");
-    }
+    if (rc == CNV_OK && cfg->test_guard_cells == 2 && s->guards.plant("s->u") != cudaSuccess)
+        rc = fail(CNV_CUDA_ERROR, "guard setup failed");  // the checker's own test: a byte after u
     if (rc != CNV_OK) {
         free_state(s);
         return rc;

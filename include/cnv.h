@@ -112,7 +112,8 @@ typedef struct cnv_config {
                                 kernel wrote there); 2 also changes one guard byte after u at
                                 creation, so the first check must report it; 0: off. Batches
                                 (cnv_batch_create's base) put a guard after every buffer of every
-                                cavity in their arena and check after each cnv_batch_step */
+                                cavity in their arena and check after each cnv_batch_step; adjoint
+                                handles check after each forward and backward run */
 } cnv_config;
 
 /* Per-step record: the values the reference logs (src/poisson.c:275, src/main.c:407-408). */

@@ -96,3 +96,28 @@ def test_batch_guard_check_reports_a_changed_byte(cnv):
         rc, _ = bt.step(1, raise_on_error=False)
         assert rc == cnv.CNV_CUDA_ERROR
         assert "after cavity 0's u" in cnv.last_error()
+
+
+# --------------------------------------------------------------------------- differentiable form
+@pytest.mark.parametrize("n,order", [(33, 6), (64, 4)])
+def test_no_adjoint_kernel_writes_outside_its_buffers(cnv, n, order):
+    """Forward run with checkpoints and the backward run's segment recomputation, with guards
+    around every field, checkpoint and segment buffer: none changed, and J and the gradients equal
+    those of the unguarded run bit for bit."""
+    w0 = cnv.noise_field(n, seed=5, sigma=1.0, passes=4)
+    out = []
+    for guards in (0, 1):
+        cfg = cnv.default_config(nx=n, ny=n, Re=400.0, dt=0.2 * min((1 / n) ** 2 * 100.0, 1 / n), order=order,
+                                 test_guard_cells=guards)
+        with cnv.Adjoint(cfg, 3) as adj:
+            out.append(adj.enstrophy_gradient(w0, 1.0, 8))
+    (j0, g0, l0), (j1, g1, l1) = out
+    assert j0 == j1 and l0 == l1 and np.array_equal(g0.view(np.uint64), g1.view(np.uint64))
+
+
+def test_adjoint_guard_check_reports_a_changed_byte(cnv):
+    cfg = cnv.default_config(nx=32, ny=32, Re=400.0, dt=1e-4, test_guard_cells=2)
+    with cnv.Adjoint(cfg, 4) as adj:
+        with pytest.raises(cnv.CnvError) as ei:
+            adj.forward(np.zeros((32, 32)), 1.0, 2)
+    assert ei.value.status == cnv.CNV_CUDA_ERROR and "after u changed" in str(ei.value)
