@@ -15,8 +15,10 @@ timed region. roofline = the persistent Poisson kernel, algorithmic bytes (24 B 
 cell per sweep: read psi and f, write psi) over its CUDA-event duration, against the measured
 HBM copy bandwidth; roofline.fp64_pipe = the same kernel's FP64 rate (7 add/multiply operations
 per cell-sweep), against the device's rate for that mix measured by a probe kernel in the same
-run -- the ceiling that binds, since the solve runs from L2. cpu_baseline = the CPU oracle (a restatement of the reference's own
-algorithm) on this host's cores for one step of the same workload.
+run -- the ceiling that binds, since the solve runs from L2. cpu_baseline = the CPU oracle (a
+restatement of the reference's own algorithm) on this host's cores for the same steps as value,
+started from the GPU's fields after the warm-up steps. config is the workload only; both arms
+print the same dict (the reference arm runs the same steps); how this arm runs it is in path.
 
 forms = the other ways the library takes the step, each timed the same way and compared field by
 field (max and RMS relative difference) after the same steps with the plain FP64 SOR path and
@@ -183,6 +185,21 @@ class ClockSampler:
                 "samples": len(sm), "power_w_max": max(power) if power else None}
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_poisson launch on the headline
+# workload, from an ncu capture of the kernel as built at the commit named below. The solve runs
+# from L2, so this is the compulsory first touch of psi and f, not a per-sweep figure.
+POISSON_TRAFFIC = {"bytes_per_launch": 19030016.0,
+                   "source": "ncu capture of k_poisson, 1024^2 workload, one launch (step 0), build of commit 4802a66"}
+
+L2_NOTE = "flushed before every timed step on the GPU (256 MB device write)"
+
+
+def bench_config(w, first_step, sweeps_per_step):
+    """The workload description both arms print (the reference arm runs the same steps)."""
+    return {"workload": workload_name(w), "grid": w["n"], "first_step": first_step,
+            "sweeps_per_step": round(sweeps_per_step, 1), "l2": L2_NOTE}
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -190,20 +207,6 @@ def measured_peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
-
-
-def profiled_traffic_per_launch():
-    """DRAM bytes (read + write) of one Poisson-kernel launch on this workload, from the
-    committed ncu summary (profiles/poisson_rb_fp64.md, line 'dram_bytes_per_launch: X'), or
-    None. The solve is L2-resident, so this is the compulsory first touch, not per sweep."""
-    path = os.path.join(ROOT, "profiles", "poisson_rb_fp64.md")
-    try:
-        for line in open(path):
-            if line.strip().startswith("dram_bytes_per_launch:"):
-                return float(line.split(":", 1)[1].split()[0])
-    except Exception:
-        pass
-    return None
 
 
 def form_adjoint(cnvpy, local, ndirs=16, n=256, steps=2000, every=100, eps=1e-6):
@@ -427,22 +430,26 @@ def run_e2e(cnvpy, w, device, steps, warmup):
     return elapsed, pinned
 
 
-def cpu_baseline(w, ncores):
-    """The CPU oracle on this host for one step (step 0) of the workload."""
-    import numpy as np
+def cpu_baseline(w, ncores, start_fields, first_step, steps, gpu_sweeps):
+    """The CPU oracle on this host for the same steps as the GPU's timed region: it starts from
+    the GPU's fields after the warm-up steps (bit for bit the oracle's own state there) and runs
+    steps first_step .. first_step + steps - 1."""
     import orc
 
     orc.build()
     n = w["n"]
     p = orc.make_params(n, re=w["re"], dt=w["dt"], u_bc=(0.0, 0.0, 0.0, w["lid"]), tol=w["tol"],
                         itmax=w["itmax"], threads=ncores, exact_norm=0)
-    W, U, V, PSI = orc.initial_state(n)
+    W, U, V, PSI = (a.copy() for a in start_fields)
     t0 = time.perf_counter()
-    rc, info = orc.run(p, 1, W, U, V, PSI)
+    rc, info = orc.run(p, steps, W, U, V, PSI)
     t1 = time.perf_counter()
-    return {"value": n * n / (t1 - t0) / 1e6, "unit": UNIT, "cores": ncores, "kind": "port",
-            "sample": f"1 time step (step 0, {info[0]['iters'] + 1} red-black SOR sweeps) of the {n}^2 workload, "
-                      f"oracle/cnv_oracle.c with OpenMP on {ncores} threads, {t1 - t0:.2f} s"}
+    sweeps = [s["iters"] + 1 for s in info]
+    return {"value": n * n * steps / (t1 - t0) / 1e6, "unit": UNIT, "cores": ncores, "kind": "port",
+            "sample": f"steps {first_step}..{first_step + steps - 1} of the {n}^2 workload (the GPU's timed "
+                      f"steps, {sum(sweeps) / len(sweeps):.1f} red-black SOR sweeps per step), "
+                      f"oracle/cnv_oracle.c with OpenMP on {ncores} threads, {t1 - t0:.2f} s",
+            "sweeps_match_gpu": sweeps == gpu_sweeps}
 
 
 def ours(args):
@@ -479,7 +486,7 @@ def ours(args):
         kernel = "k_poisson (persistent red-black SOR, one launch per step)"
     achieved = alg_bytes / (pms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = profiled_traffic_per_launch() if args.form == "fp64" else None
+    traffic = POISSON_TRAFFIC["bytes_per_launch"] if args.form == "fp64" else None
     fp64 = None
     if args.form == "fp64":
         # the binding ceiling: the update's 7 FP64 add/multiply operations per interior cell-sweep
@@ -518,20 +525,22 @@ def ours(args):
         forms["adjoint_256"] = form_adjoint(cnvpy, local)
 
     cpu = None
-    if rank == 0 and ws == 1 and not args.skip_cpu:
-        cpu = cpu_baseline(w, os.cpu_count() or 1)
+    if rank == 0 and ws == 1 and not args.skip_cpu and args.form == "fp64":
+        start = run_device(cnvpy, w, local, args.warmup, 0, lambda: None, fields=True)[1]
+        cpu = cpu_baseline(w, os.cpu_count() or 1, start, args.warmup, args.steps,
+                           [r["iters"] + 1 for r in recs])
 
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms_max / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(w), "grid": w["n"], "precision": prec_name,
-                   "l2": "flushed before every timed step (256 MB device write)" if flush.active else "not flushed",
-                   "parallelism": f"replicas x{ws}", "sweeps_per_step": round(sweeps / len(recs), 1),
-                   "first_step": args.warmup, "solver": recs[0]["solver"] if recs else None},
+        "config": bench_config(w, args.warmup, sweeps / len(recs)),
+        "path": {"precision": prec_name, "solver": recs[0]["solver"] if recs else None,
+                 "parallelism": f"replicas x{ws}", "l2_flushed": flush.active},
         "Mcell_sweeps_per_s": round(interior * sweeps / (pms * 1e-3) / 1e6, 2),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "traffic_source": POISSON_TRAFFIC["source"] if traffic else None, "peak_source": peak_kind,
                      "kernel": kernel, "fp64_pipe": fp64},
         "e2e": e2e,
         "gpu_launches": 5 * args.steps,
@@ -575,8 +584,7 @@ def reference(args):
         "impl": "reference", "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round((t1 - t0) * 1e3 / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(w), "grid": n,
-                   "sweeps_per_step": round(sum(s["iters"] + 1 for s in info) / len(info), 1)},
+        "config": bench_config(w, args.warmup, sum(s["iters"] + 1 for s in info) / len(info)),
         "cpu_baseline": {"value": round(value, 6), "unit": UNIT, "cores": cores, "kind": kind,
                          "sample": f"steps {args.warmup}..{args.warmup + args.steps - 1} of the {n}^2 workload, "
                                    f"oracle/cnv_oracle.c (restatement of the reference's CPU path, red-black "

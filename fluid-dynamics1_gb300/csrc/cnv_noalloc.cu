@@ -7,8 +7,16 @@
 // cnv_create allocates the working buffers. cnv_poisson_noalloc takes only the caller's input
 // and output arrays and keeps every intermediate array (the two red/black copies of psi, the
 // red/black right-hand side, the solver's synchronisation block, the control block) in the
-// file-scope array g_scratch below. The array is placed in device memory when the library's module is loaded,
-// and every GPU that loads the library keeps it until the process exits.
+// file-scope array g_scratch below.
+//
+// When the array is placed: the library's device code is compiled without relocatable device
+// code, so g_scratch sits in a module of its own. With CUDA's default lazy module loading, that
+// module (and the solver kernels' modules) are loaded onto a device when this entry point
+// first runs there: the FIRST call on each device takes device memory for the array (about
+// 6.3 MB) and the kernels' code. Callers make one warm-up call per device at start-up, before
+// their memory pool owns the device and outside any stream capture; later calls allocate
+// nothing. With CUDA_MODULE_LOADING=EAGER everything is placed when the library loads. Every
+// device that has loaded the array keeps it until the process exits.
 //
 // Limits and sharing rules:
 //   - grids up to kMaxN x kMaxN (512 x 512); larger n is rejected with CNV_BAD_ARG;
@@ -17,14 +25,15 @@
 //     synchronisation block), so back-to-back calls
 //     are independent, but two calls whose GPU work overlaps (different streams or host
 //     threads at the same time) race on the same memory and give wrong results.
-//   - the first call on each device looks up the device address of g_scratch with
-//     cudaGetSymbolAddress (with that device current) and caches it; make that first call
-//     outside any stream capture.
+//   - in host code g_scratch names a host-side stand-in, not device memory. Every call looks
+//     up the array's device address on the current device with cudaGetSymbolAddress and
+//     passes that to the kernels. The lookup is cheap once the module is loaded, and not
+//     caching it keeps the entry point valid after the caller resets the device's context
+//     (cudaDeviceReset), which frees the old array.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "cnv_kernels.h"
 
@@ -41,10 +50,6 @@ constexpr size_t kScratchBytes = kCtrlBytes + kSyncBytes + 6 * kSplitBytes;
 static_assert(sizeof(Ctrl) <= kCtrlBytes, "control block does not fit its slot");
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-unsigned char* g_scratch_addr[kMaxDevices] = {};
 
 // This entry point has no state to hold an error string, so it reports why it failed on stderr
 // and returns the status code.
@@ -74,18 +79,14 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
     cudaStream_t stream = static_cast<cudaStream_t>(stream_handle);
 
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-        return error(CNV_NO_DEVICE, "no current CUDA device");
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return error(CNV_NO_DEVICE, "no current CUDA device");
+    // the device address of g_scratch on the current device (loads its module on the first call)
     unsigned char* base = nullptr;
     {
-        std::lock_guard<std::mutex> lock(g_mutex);
-        if (!g_scratch_addr[dev]) {
-            void* p = nullptr;
-            const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-            if (e != cudaSuccess || !p) return error(CNV_CUDA_ERROR, cudaGetErrorString(e));
-            g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-        }
-        base = g_scratch_addr[dev];
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+        if (e != cudaSuccess || !p) return error(CNV_CUDA_ERROR, cudaGetErrorString(e));
+        base = static_cast<unsigned char*>(p);
     }
     Ctrl* ctrl = reinterpret_cast<Ctrl*>(base);
     void* sync = base + kCtrlBytes;

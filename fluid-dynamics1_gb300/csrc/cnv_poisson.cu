@@ -25,9 +25,10 @@
 // frame's latency is covered by the other warps' interior work and the FP64 pipe never idles
 // on a block-wide barrier. There is no grid-wide barrier.
 //
-// Stop test. Each block adds its partial sum of |dpsi| to a 128-bit fixed-point accumulator
-// (scale 2^80, kept as four 32-bit chunks in 64-bit counters: exact integer adds with no carry,
-// so the total is independent of arrival order) in a ring of 8 slots, and counts itself in. The
+// Stop test. Each block adds its partial sum of |dpsi| to a fixed-point accumulator (units of
+// 2^-80, kept as four 32-bit chunks in 64-bit counters: exact integer adds with no carry, so the
+// total is independent of arrival order; cells with |psi| >= 2^46 go to an FP64 side sum) in a
+// ring of 8 slots, and counts itself in. The
 // signal warp checks e_{k-2} while the other warps finish sweep k-1 and posts the verdict at
 // barrier DEC before sweep k; if e_{k-2} < tol every block stops before overwriting set
 // (k-2)&1, which holds the answer. The extra sweep k-1 is discarded. Every wait of the signal
@@ -88,14 +89,16 @@ struct SyncState {
     // that every contribution is a fire-and-forget add with no carry between words
     unsigned long long acc[kRing][4];
     unsigned int count[kRing];
-    unsigned int nonfinite[kRing];
+    unsigned int fp64[kRing];   // a block added an FP64 part (cells with |psi| >= 2^46) to fsum
+    double fsum[kRing];
     unsigned int flag[2][kMaxSolverBlocks];  // [colour][block]: last sweep whose frame is written
 };
 
 // Block-shared state of the two warp roles.
 struct Shared {
     unsigned long long part[2][kCellWarps][4];  // [sweep parity][warp] norm chunk sums
-    unsigned int pbig[2][kCellWarps];
+    unsigned int pfp[2][kCellWarps];             // the warp's FP64 part of the norm is pfs
+    double pfs[2][kCellWarps];
     unsigned int ctr[2];                        // interior chunk counters, by half-sweep parity
     int stop[2];                                // verdict before sweep k, at [k & 1]
     int status, conv_k;
@@ -301,14 +304,21 @@ __device__ __forceinline__ void frame_pass(const PoissonParams& p, const Tile& t
 // in sh.part[k & 1]) to ring slot k % kRing and counts the block in.
 __device__ __forceinline__ void contribute(SyncState* sy, int k, const Shared& sh) {
     unsigned long long s[4] = {0, 0, 0, 0};
-    unsigned big = 0;
+    unsigned fp = 0;
+    double fs = 0.0;
     for (int w = 0; w < kCellWarps; ++w) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) s[c] += sh.part[k & 1][w][c];
-        big |= sh.pbig[k & 1][w];
+        if (sh.pfp[k & 1][w]) {
+            fp = 1;
+            fs = __dadd_rn(fs, sh.pfs[k & 1][w]);
+        }
     }
     const int slot = k % kRing;
-    if (big) atomicOr(&sy->nonfinite[slot], 1u);
+    if (fp) {
+        atomicAdd(&sy->fsum[slot], fs);
+        atomicOr(&sy->fp64[slot], 1u);
+    }
 #pragma unroll
     for (int c = 0; c < 4; ++c) atomicAdd(&sy->acc[slot][c], s[c]);
     __threadfence();
@@ -323,17 +333,9 @@ __device__ int check_norm(SyncState* sy, int j, const PoissonParams& p, Ctrl* ct
     unsigned long long c[4];
 #pragma unroll
     for (int w = 0; w < 4; ++w) c[w] = __ldcg(&sy->acc[slot][w]);
-    // carry-propagate the 32-bit chunks into a 128-bit value
-    unsigned long long t = c[0];
-    unsigned long long lo = t & 0xffffffffull;
-    t = c[1] + (t >> 32);
-    lo |= (t & 0xffffffffull) << 32;
-    t = c[2] + (t >> 32);
-    unsigned long long hi = t & 0xffffffffull;
-    t = c[3] + (t >> 32);
-    hi |= t << 32;
-    *e = from_fixed96(lo, hi);
-    if (__ldcg(&sy->nonfinite[slot]) || !isfinite(*e)) return 3;
+    *e = norm_total(c);
+    if (__ldcg(&sy->fp64[slot])) *e = __dadd_rn(*e, __ldcg(&sy->fsum[slot]));
+    if (!isfinite(*e)) return 3;
     return *e < p.tol ? 1 : 0;
 }
 
@@ -365,7 +367,8 @@ __device__ void signal_warp(const PoissonParams& p, const Tile& t, SyncState* sy
                 const int slot = (k - 4) % kRing;
 #pragma unroll
                 for (int w = 0; w < 4; ++w) sy->acc[slot][w] = 0;
-                sy->nonfinite[slot] = 0;
+                sy->fp64[slot] = 0;
+                sy->fsum[slot] = 0.0;
                 __threadfence();
                 atomicExch(&sy->count[slot], 0u);
             }
@@ -460,7 +463,7 @@ __device__ void cell_warps(const PoissonLaunch& L, const Tile& t, Shared& sh) {
         q.next[1] = odd ? s1b : s0b;
         q.rhs[0] = L.rhs[0];
         q.rhs[1] = L.rhs[1];
-        NormAcc acc{{0, 0, 0, 0}, 0};
+        NormAcc acc{{0, 0, 0, 0}, 0, 0.0};
         if (KIND == CNV_POISSON_JACOBI) {
             q.oth[0] = q.prev[1];
             q.oth[1] = q.prev[0];
@@ -508,11 +511,18 @@ __device__ void cell_warps(const PoissonLaunch& L, const Tile& t, Shared& sh) {
             for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
             acc.c[w] = x;
         }
-        const unsigned big = __any_sync(0xffffffffu, acc.big) ? 1u : 0u;
+        const unsigned fp = __any_sync(0xffffffffu, acc.fp64) ? 1u : 0u;
+        double fs = 0.0;
+        if (fp) {  // only where a cell reached 2^46: the FP64 part, summed over the warp
+            fs = acc.fsum;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) fs = __dadd_rn(fs, __shfl_xor_sync(0xffffffffu, fs, off));
+        }
         if ((threadIdx.x & 31) == 0) {
 #pragma unroll
             for (int w = 0; w < 4; ++w) sh.part[k & 1][warp][w] = acc.c[w];
-            sh.pbig[k & 1][warp] = big;
+            sh.pfp[k & 1][warp] = fp;
+            sh.pfs[k & 1][warp] = fs;
         }
         __syncwarp();
         bar_arrive(kBarNorm, kThreads);

@@ -10,52 +10,100 @@
 namespace cnv {
 namespace {
 
-// exact 128-bit fixed-point image (scale 2^80, truncated) of a non-negative double
-__device__ __forceinline__ void to_fixed96(double x, unsigned long long& lo, unsigned long long& hi) {
-    lo = hi = 0;
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const int ex = (int)((b >> 52) & 0x7ff);
-    if (ex == 0 || ex == 0x7ff || (b >> 63)) return;  // zero, subnormal (< 2^-1022), inf/nan, negative
-    const unsigned long long mant = (b & ((1ull << 52) - 1)) | (1ull << 52);
-    const int s = ex - 1075 + 80;  // value * 2^80 = mant * 2^s
-    if (s >= 64 + 11) {            // would not fit 128 bits: saturate
-        lo = ~0ull;
-        hi = ~0ull >> 1;
-    } else if (s >= 64) {
-        hi = mant << (s - 64);
-    } else if (s > 0) {
-        lo = mant << s;
-        hi = mant >> (64 - s);
-    } else if (s > -53) {
-        lo = mant >> (-s);
+// (x2:hi:lo) * 2^-80 rounded to the nearest double, ties to even, where x2 holds bits 128..191:
+// the stop norm's fixed-point total converted with one correct rounding (such values are normal).
+__host__ __device__ __forceinline__ double fixed80_to_double(unsigned long long lo, unsigned long long hi,
+                                                             unsigned long long x2) {
+    bool sticky = false;  // non-zero bits below lo after a renormalisation
+    int scale = -80;
+    if (x2) {
+        sticky = lo != 0;
+        lo = hi;
+        hi = x2;
+        scale += 64;
     }
+    if ((lo | hi) == 0) return 0.0;
+#ifdef __CUDA_ARCH__
+    const int top = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)lo);  // leading bit
+#else
+    const int top = hi ? 127 - __builtin_clzll(hi) : 63 - __builtin_clzll(lo);
+#endif
+    const int drop = top - 52;  // bits below the 53-bit significand
+    unsigned long long m;
+    bool up = false;
+    if (drop <= 0) {
+        m = lo << (-drop);  // top <= 52: hi == 0, exact (no sticky bits: x2 was 0)
+    } else {
+        unsigned long long rh, rl;  // the dropped bits
+        if (drop >= 64) {
+            const int d = drop - 64;
+            m = hi >> d;
+            rh = d ? hi & ((1ull << d) - 1) : 0;
+            rl = lo;
+        } else {
+            m = (lo >> drop) | (hi << (64 - drop));
+            rh = 0;
+            rl = lo & ((1ull << drop) - 1);
+        }
+        const unsigned long long hh = drop - 1 >= 64 ? 1ull << (drop - 65) : 0;  // half an ulp
+        const unsigned long long hl = drop - 1 >= 64 ? 0 : 1ull << (drop - 1);
+        const bool eq = rh == hh && rl == hl;
+        const bool gt = rh > hh || (rh == hh && rl > hl) || (eq && sticky);
+        up = gt || (eq && !sticky && (m & 1));
+    }
+    m += up ? 1 : 0;
+    int e = top;
+    if (m >> 53) {  // rounded up to the next power of two
+        m >>= 1;
+        ++e;
+    }
+    const unsigned long long bits = ((unsigned long long)(e + scale + 1023) << 52) | (m & ((1ull << 52) - 1));
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)bits);
+#else
+    double out;
+    __builtin_memcpy(&out, &bits, sizeof out);
+    return out;
+#endif
 }
 
-__device__ __forceinline__ double from_fixed96(unsigned long long lo, unsigned long long hi) {
-    return (double)hi * 0x1.0p-16 + (double)lo * 0x1.0p-80;
+// The stop norm from its four 32-bit chunk counters (chunk w holds bits 32w.. of the total in
+// units of 2^-80, each counter up to 2^64): carry-propagate into a 160-bit integer and convert.
+__host__ __device__ __forceinline__ double norm_total(const unsigned long long c[4]) {
+    unsigned long long t = c[0];
+    unsigned long long lo = t & 0xffffffffull;
+    t = c[1] + (t >> 32);
+    lo |= (t & 0xffffffffull) << 32;
+    t = c[2] + (t >> 32);
+    unsigned long long hi = t & 0xffffffffull;
+    t = c[3] + (t >> 32);
+    hi |= (t & 0xffffffffull) << 32;
+    return fixed80_to_double(lo, hi, t >> 32);
 }
 
-// Stop-norm accumulator of one thread: |psi_new - psi_old| summed exactly as integers in units
-// of 2^-80, in four 32-bit chunks held by 64-bit counters (no carries while accumulating).
+// Stop-norm accumulator of one thread. |psi_new - psi_old| is summed exactly as integers in
+// units of 2^-80, in four 32-bit chunks held by 64-bit counters (no carries while accumulating),
+// for every cell whose two values lie below 2^46 in magnitude. Each value is truncated to a
+// multiple of 2^-80 first: values of 2^-28 or more are multiples already, so a cell is off by
+// less than 2^-80 only when one of its values lies below 2^-28, and the total is off by less than
+// (number of cells) * 2^-80 (about 1e-18 at 1024^2). Cells with a value of 2^46 or more (or a
+// non-finite one) are summed in FP64 instead (fsum, flagged by fp64): they are far outside any
+// realistic streamfunction, and the reference sums them in FP64 too.
 struct NormAcc {
     unsigned long long c[4];
-    unsigned int big;  // set if a value reached 2^46 (outside the fixed-point range)
+    unsigned int fp64;  // set once fsum holds a cell
+    double fsum;
 };
 
-// |x| * 2^80, truncated, as a 128-bit integer (hi:lo); values below 2^-80 give 0.
-__device__ __forceinline__ void abs_fixed80(double x, unsigned long long& lo, unsigned long long& hi,
-                                            unsigned int& big) {
+// |x| * 2^80, truncated, as a 128-bit integer (hi:lo), for |x| < 2^46; values below 2^-80 give 0.
+__device__ __forceinline__ void abs_fixed80(double x, unsigned long long& lo, unsigned long long& hi) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
     const int ex = (int)(b >> 52);
     const unsigned long long mant = (b & ((1ull << 52) - 1)) | (1ull << 52);
-    const int s = ex - 995;  // |x| * 2^80 = mant * 2^s
+    const int s = ex - 995;  // |x| * 2^80 = mant * 2^s, s < 74
     lo = 0;
     hi = 0;
     if (ex == 0) return;     // zero or below 2^-1022
-    if (s >= 74) {           // |x| >= 2^46 (also inf/nan)
-        big = 1;
-        return;
-    }
     if (s >= 64) {
         hi = mant << (s - 64);
     } else if (s > 0) {
@@ -66,7 +114,8 @@ __device__ __forceinline__ void abs_fixed80(double x, unsigned long long& lo, un
     }
 }
 
-// acc += |nw - old|, exactly in fixed point (both truncated at 2^-80), on the integer pipes.
+// acc += |nw - old|: exactly in fixed point (both truncated at 2^-80) on the integer pipes, or in
+// FP64 when a value reaches 2^46.
 __device__ __forceinline__ void norm_add(NormAcc& acc, double nw, double old) {
     {
         // the common case, same sign and exponent e with 2^-28 <= |x| < 2^46: both images are
@@ -97,9 +146,16 @@ __device__ __forceinline__ void norm_add(NormAcc& acc, double nw, double old) {
             return;
         }
     }
+    if (((unsigned long long)__double_as_longlong(nw) & 0x7fffffffffffffffull) >= (1069ull << 52) ||
+        ((unsigned long long)__double_as_longlong(old) & 0x7fffffffffffffffull) >= (1069ull << 52)) {
+        // a value of 2^46 or more, Inf or NaN: the FP64 part of the norm
+        acc.fsum = __dadd_rn(acc.fsum, fabs(__dsub_rn(nw, old)));
+        acc.fp64 = 1;
+        return;
+    }
     unsigned long long al, ah, bl, bh;
-    abs_fixed80(nw, al, ah, acc.big);
-    abs_fixed80(old, bl, bh, acc.big);
+    abs_fixed80(nw, al, ah);
+    abs_fixed80(old, bl, bh);
     unsigned long long dl, dh;
     if ((__double_as_longlong(nw) ^ __double_as_longlong(old)) < 0) {  // opposite signs: |a| + |b|
         dl = al + bl;

@@ -187,11 +187,19 @@ int cnv_poisson_device(cnv_state *s, const double *f, double *psi, int *iters, d
  * CNV_POISSON_GS, CNV_POISSON_SOR or CNV_POISSON_JACOBI; precision CNV_PREC_FP64 or
  * CNV_PREC_FP64_FMA; beta <= 0 selects the reference SOR factor for n. iters/err may be NULL.
  * Working arrays live in one fixed array in device memory (about 6.3 MB, held by every GPU
- * that loads the library until the process exits), so n is limited to 512: larger n returns
+ * that has loaded it until the process exits), so n is limited to 512: larger n returns
  * CNV_BAD_ARG with a message on stderr. All calls on a device share that array: calls whose
  * GPU work overlaps (other streams or host threads at the same time) race and must be
- * serialised by the caller. The first call on each device sets up the array's address; make
- * it before any stream capture. */
+ * serialised by the caller.
+ * First call on a device: with CUDA's default lazy module loading (CUDA_MODULE_LOADING=LAZY)
+ * the array and the solver's kernels are placed on a device when this entry point first runs
+ * there, so that first call DOES take device memory (the 6.3 MB array plus the kernels' code).
+ * Make one warm-up call on each device at start-up, before the caller's memory pool takes the
+ * device and outside any stream capture; every later call allocates nothing. Setting
+ * CUDA_MODULE_LOADING=EAGER in the environment places everything when the library loads.
+ * Each call looks up the array's device address again (cudaGetSymbolAddress), so the entry
+ * point keeps working after the caller resets the device's context (cudaDeviceReset); the
+ * next call after such a reset is a first call again. */
 int cnv_poisson_noalloc(const double *f, double *psi, int n, double dx, double dy,
                         int poisson_type, int precision, double beta, int itmax, double tol,
                         int *iters, double *err, void *stream);

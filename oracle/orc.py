@@ -41,12 +41,20 @@ class StepInfo(C.Structure):
                 ("cont_min", C.c_double), ("status", C.c_int)]
 
 
+def reference_tree() -> str | None:
+    """The reference's source tree, or None where it is absent: $CNV_REFERENCE_TREE when set,
+    else a checkout named ``reference`` beside this repository (the same rule as oracle/Makefile)."""
+    ref = os.environ.get("CNV_REFERENCE_TREE") or os.path.join(os.path.dirname(HERE), "..", "reference")
+    ref = os.path.abspath(ref)
+    return ref if os.path.isdir(os.path.join(ref, "src")) else None
+
+
 def build(force: bool = False) -> None:
     """Compile liboracle.so (and the reference harness when the reference tree exists)."""
     if force or not os.path.exists(LIB_PATH):
         subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    ref = os.environ.get("CNV_REFERENCE_TREE", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "src")) and (force or not os.path.exists(REF_LIB_PATH)):
+    ref = reference_tree()
+    if ref and (force or not os.path.exists(REF_LIB_PATH)):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True)
 
 

@@ -11,7 +11,8 @@ on the same configurations truncated to a few steps, and checks that its fresh l
 the shipped lines, so the fixtures are pinned to the code, not only to the files.
 
 Run from the repository root:  python tests/golden/make_golden.py [--verify]
-This script needs the reference tree; the fixtures it writes do not.
+This script needs the reference tree ($CNV_REFERENCE_TREE, or a checkout named "reference" beside
+this repository); the fixtures it writes do not.
 """
 from __future__ import annotations
 
@@ -23,9 +24,10 @@ import subprocess
 import sys
 import tempfile
 
-REF = os.environ.get("CNV_REFERENCE_TREE", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
+# the reference tree: $CNV_REFERENCE_TREE, else a checkout named "reference" beside this repository
+REF = os.path.abspath(os.environ.get("CNV_REFERENCE_TREE") or os.path.join(ROOT, "..", "reference"))
 
 # Run configurations: config_default.txt (64^2, Re 1000, dt 0.005, tol 1e-3, itmax 10000) and
 # config_high_re.txt (128^2, Re 5000, dt 1e-3, tol 5e-4, itmax 15000); openmp_enabled selects

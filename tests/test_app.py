@@ -143,8 +143,10 @@ def test_reference_program_links_against_compat_library():
     src/poisson.c and src/fluiddyn.c, in both of the reference's builds: the compatibility library
     defines every function the program takes from those two files. The programs only print their
     usage here (no GPU)."""
-    ref = os.environ.get("CNV_REFERENCE_TREE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src")):
+    import orc  # the oracle's helpers locate the reference tree
+
+    ref = orc.reference_tree()
+    if ref is None:
         pytest.skip("reference tree absent")
     import build as product_build  # fluid-dynamics1_gb300/build.py
 

@@ -210,6 +210,37 @@ def test_1024_four_steps_match_oracle(cnv, orc):
         assert bitwise(a, b), name
 
 
+@pytest.mark.parametrize("blocking", [1, 4])
+@pytest.mark.parametrize("ptype", [1, 2])
+def test_poisson_with_streamfunction_beyond_2_46(cnv, orc, ptype, blocking):
+    """A right-hand side scaled by 2^70 drives |psi| far past 2^46, where the stop norm's cells
+    leave the fixed-point sum for its FP64 part. Scaling by a power of two is exact in every
+    operation of the update, so the solve must give exactly 2^70 times the unscaled iterates:
+    the same sweep count (tol scaled too) and psi bit for bit; and it must equal the oracle,
+    which sums the norm in FP64 throughout, as the reference does."""
+    n = 64
+    scale = 2.0 ** 70
+    rng = np.random.default_rng(4646 + ptype)
+    f = rng.standard_normal((n, n))
+    tol = 1e-9
+    out = []
+    for s in (1.0, scale):
+        cfg = make_cfg(cnv, n, poisson_type=ptype, poisson_tol=tol * s, poisson_max_it=200000, sor_blocking=blocking)
+        with cnv.Cavity(cfg) as cav:
+            out.append(cav.poisson(f * s))
+    (rc_a, psi_a, it_a, err_a), (rc_b, psi_b, it_b, err_b) = out
+    assert rc_a == 0 and rc_b == 0, (rc_a, rc_b)
+    assert np.max(np.abs(psi_b)) >= 2.0 ** 46
+    assert it_b == it_a
+    assert bitwise(psi_b, psi_a * scale)
+    assert abs(err_b - err_a * scale) <= REL_ERR_TOL * err_a * scale
+    p = oracle_params(orc, make_cfg(cnv, n, poisson_type=ptype, poisson_tol=tol * scale, poisson_max_it=200000))
+    opsi, oit, oerr, orc_rc = orc.poisson(p, f * scale)
+    assert orc_rc == 0 and oit == it_b
+    assert bitwise(psi_b, opsi)
+    assert abs(err_b - oerr) <= REL_ERR_TOL * oerr
+
+
 # ------------------------------------------------------------------------- failure paths
 @pytest.mark.parametrize("kind", [2, 3], ids=["sor", "jacobi"])
 def test_stalled_block_times_out_and_device_stays_usable(cnv, kind):

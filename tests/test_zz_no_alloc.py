@@ -7,7 +7,10 @@ point keeps its working arrays in one fixed device array inside the library. The
 it through the C ABI twice in a row, on different right-hand sides, and compare each result
 with the regular entry point (cnv_poisson_device on a cnv_state). They use the same
 tolerance as the other parity tests: fields to 1e-12 normwise relative (the two paths run the
-same kernels, so they normally agree bit for bit) and equal iteration counts.
+same kernels, so they normally agree bit for bit) and equal iteration counts. A further test
+checks the property the entry point exists for: once a first call has run on the device (that
+call loads the library's kernels and places the fixed array there, under CUDA's default lazy
+module loading), a call leaves the device's free memory unchanged.
 
 This file is named so that pytest collects it last.
 """
@@ -57,6 +60,33 @@ def test_noalloc_matches_state_entry_point_on_two_calls(cnv, n, ptype, precision
             assert np.max(np.abs(a - b)) <= FIELD_TOL * np.max(np.abs(b)), f"call {call}"
             assert it_a == it_b.value, f"call {call}"
             assert abs(err_a - err_b.value) <= FIELD_TOL * abs(err_b.value), f"call {call}"
+
+
+@pytest.mark.gpu
+def test_noalloc_call_after_the_first_takes_no_device_memory(cnv):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    n = 256
+    h = 1.0 / n
+    gen = torch.Generator(device="cpu").manual_seed(7)
+    f = torch.randn((n, n), dtype=torch.float64, generator=gen).cuda()
+    psi = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    # first call on this device: may load modules and place the fixed array
+    assert _solve_noalloc(cnv, torch, f, psi, n, h, 2, 0)[0] == 0
+    torch.cuda.synchronize()
+    results = []
+    for _ in range(2):
+        free_before, _total = torch.cuda.mem_get_info()
+        rc, it, _err = _solve_noalloc(cnv, torch, f, psi, n, h, 2, 0)
+        torch.cuda.synchronize()
+        free_after, _total = torch.cuda.mem_get_info()
+        assert rc == 0
+        assert free_after == free_before, f"device free memory changed by {free_before - free_after} bytes"
+        results.append((it, psi.cpu().numpy().copy()))
+    assert results[0][0] == results[1][0]
+    assert np.array_equal(results[0][1], results[1][1])
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch_size(cnv):
