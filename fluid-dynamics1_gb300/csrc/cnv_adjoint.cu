@@ -254,6 +254,7 @@ StepArgs base_args(const cnv_adjoint* a) {
     s.sor[0] = a->sor[0];
     s.sor[1] = a->sor[1];
     s.ctrl = a->ctrl;
+    s.timeout_ns = 2000000000LL;
     return s;
 }
 
@@ -267,12 +268,11 @@ int forward_step(cnv_adjoint* a, double* w_in, const double* u_in, const double*
     s.w_out = w_out;
     s.u = const_cast<double*>(u_in);
     s.v = const_cast<double*>(v_in);
-    ACUDA(launch_wall(s, a->stream));
-    ACUDA(launch_transport(s, a->stream));
+    ACUDA(launch_pre(s, a->stream));
     ACUDA(dst_solve_split(a->dst, w_out, a->c4, a->sor[0], a->sor[1], a->pitch, a->stream));
     s.u = u_out;
     s.v = v_out;
-    ACUDA(launch_velocity(s, a->stream));
+    ACUDA(launch_post(s, false, a->stream));
     return CNV_OK;
 }
 

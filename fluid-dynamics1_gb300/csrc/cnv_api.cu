@@ -368,20 +368,16 @@ int enqueue_poisson(cnv_state* s, const double* in, double scale, bool in_step) 
     return CNV_OK;
 }
 
-// The step is three stream segments: graph[0][parity] (wall + transport passes), the Poisson
-// solve (memsets + one cooperative launch, bracketed by timing events), and graph[1][parity]
-// (velocity + continuity passes).
+// The step is three stream segments: graph[0][parity] (the pre-solve pass: wall, transport,
+// right-hand side), the Poisson solve (memsets + one cooperative launch, bracketed by timing
+// events), and graph[1][parity] (the post-solve pass: velocity and continuity).
 int enqueue_pre(cnv_state* s, int parity) {
-    const StepArgs a = step_args(s, parity);
-    CNV_CUDA(launch_wall(a, s->stream));
-    CNV_CUDA(launch_transport(a, s->stream));
+    CNV_CUDA(launch_pre(step_args(s, parity), s->stream));
     return CNV_OK;
 }
 
 int enqueue_post(cnv_state* s, int parity) {
-    const StepArgs a = step_args(s, parity);
-    CNV_CUDA(launch_velocity(a, s->stream));
-    CNV_CUDA(launch_continuity(a, s->stream));
+    CNV_CUDA(launch_post(step_args(s, parity), true, s->stream));
     return CNV_OK;
 }
 
@@ -513,7 +509,11 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
         s->poisson_grid = std::min(cfg->solver_blocks, std::min(std::min(per_sm, 2) * s->sms, kMaxSolverBlocks));
     poisson_tiles(n, s->poisson_grid, &s->poisson_gx, &s->poisson_gy);
     s->poisson_grid = s->poisson_gx * s->poisson_gy;
-    s->cont_blocks = (int)std::max(1LL, std::min<long long>(2LL * s->sms, (long long)(nn + 255) / 256));
+    s->cont_blocks = post_grid(n, s->device);
+    if (s->cont_blocks < 1) {
+        free_state(s);
+        return fail(CNV_CUDA_ERROR, "occupancy query failed for the post-solve pass");
+    }
     {
         cudaError_t e_ = cudaMalloc(&s->sync, poisson_sync_bytes());
         if (e_ != cudaSuccess) {
@@ -521,7 +521,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
             return fail(CNV_CUDA_ERROR, "cudaMalloc: %s", cudaGetErrorString(e_));
         }
     }
-    ALLOC(s->cont_partials, 2 * (size_t)s->cont_blocks);
+    ALLOC(s->cont_partials, 4 * (size_t)s->cont_blocks);
     if (cfg->precision == CNV_PREC_MIXED) {
         // one block per SM; the tile plus its halo must fit in shared memory
         s->mixed = true;
@@ -662,6 +662,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     a.ctrl = s->ctrl;
     a.cont_partials = s->cont_partials;
     a.cont_blocks = s->cont_blocks;
+    a.timeout_ns = p.timeout_ns;
 
     if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess ||
         cudaEventCreate(&s->evp0) != cudaSuccess || cudaEventCreate(&s->evp1) != cudaSuccess) {

@@ -57,7 +57,7 @@ struct StepRecord {
 static_assert(sizeof(StepRecord) == sizeof(cnv_step_info), "StepRecord must mirror cnv_step_info");
 
 struct Ctrl {
-    unsigned int bar_count;   // grid barrier arrivals (zeroed before each solver launch)
+    unsigned int bar_count;   // grid barrier arrivals of the post-solve pass (re-armed by its last block)
     unsigned int cont_ticket; // last-block ticket of the continuity reduction
     int abort;                // non-zero after a failed step: later kernels return at once
     int step;                 // index of the current step within the cnv_step call

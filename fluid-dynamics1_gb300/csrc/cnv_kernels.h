@@ -31,14 +31,19 @@ struct StepArgs {
     int rhs_den_pow2;
     double rhs_inv_h2;
     Ctrl* ctrl;
-    double* cont_partials;     // 2 * cont_blocks doubles
-    int cont_blocks;
+    double* cont_partials;     // 4 * cont_blocks doubles
+    int cont_blocks;           // blocks of the post pass's cooperative launch (post_grid)
+    long long timeout_ns;      // bound on the post pass's grid barrier
 };
 
-cudaError_t launch_wall(const StepArgs& a, cudaStream_t s);
-cudaError_t launch_transport(const StepArgs& a, cudaStream_t s);
-cudaError_t launch_velocity(const StepArgs& a, cudaStream_t s);
-cudaError_t launch_continuity(const StepArgs& a, cudaStream_t s);
+// Pre-solve pass: wall vorticity, derivatives, Euler update (w_in -> w_out, wall values into
+// w_in) and the Poisson right-hand side (when rhs[0] is set).
+cudaError_t launch_pre(const StepArgs& a, cudaStream_t s);
+// Post-solve pass: u, v and row-major psi from the split-layout psi in sor[]; with continuity,
+// also the continuity max/min and the step record (a cooperative launch of cont_blocks blocks).
+cudaError_t launch_post(const StepArgs& a, bool continuity, cudaStream_t s);
+// Blocks of the post pass's cooperative launch for an n x n grid on `device` (0 on failure).
+int post_grid(int n, int device);
 // Copy a row-major field into the split layout and back (parity tests of the solver alone).
 // to_split applies the same right-hand-side scaling as the transport pass (a.c4, a.rhs_mode).
 cudaError_t launch_to_split(const double* f, double* r, double* b, const StepArgs& a, cudaStream_t s);

@@ -1,10 +1,11 @@
-// cnv_step_kernels.cu -- the non-Poisson part of cnavier's time step on the GPU.
+// cnv_step_kernels.cu -- the non-Poisson part of cnavier's time step on the GPU, as two fused
+// passes around the Poisson solve.
 //
-//   wall pass       wall vorticity on the four edges          src/main.c:298-320
-//   transport pass  DX/DY/DX2/DY2 of w + Euler update          src/main.c:323-344,
-//                   + Poisson right-hand side (f = -w)        src/fluiddyn.c:71-102, :347-348
-//   velocity pass   u = DY psi, v = -(DX psi)                  src/main.c:366-383
-//   continuity pass DX u + DY v, max and min                   src/main.c:387-408
+//   k_pre   wall vorticity on the four edges                    src/main.c:298-320
+//           + DX/DY/DX2/DY2 of w and the Euler update           src/main.c:323-344, src/fluiddyn.c:71-102
+//           + the Poisson right-hand side (f = -w)              src/main.c:347-348
+//   k_post  u = DY psi, v = -(DX psi)                           src/main.c:366-383
+//           + continuity DX u + DY v, its max and min           src/main.c:387-408
 //
 // Every arithmetic operation uses the round-to-nearest intrinsics (__dadd_rn, __dmul_rn, ...),
 // which the compiler never contracts into FMAs, in the reference's evaluation order, so these
@@ -12,13 +13,41 @@
 // reference become 7-tap bands summed from 0.0 in ascending column order (the skipped
 // products are exact zeros). Velocity Dirichlet values (src/main.c:283-296) are applied on
 // read: u and v keep the values the velocity pass wrote, as in the reference between steps.
+//
+// k_pre. One block per 32 x 32 tile. The block stages w on its tile plus the radius-3 halo of
+// the order-6 stencils in shared memory; cells on the grid's edge hold the new wall vorticity
+// there, which the block computes itself from u and v wherever its tile or halo touches an edge
+// (so no block reads another block's wall values). Each thread then takes four cells of one
+// column: the four derivatives from shared memory, u and v at the cell (coalesced global
+// loads), the Euler update, and the writes: w_out, the right-hand side in the solver's split
+// layout, and on edge cells the wall value into w_in (the reference's w after the wall loop,
+// which the adjoint form keeps).
+//
+// k_post. Persistent and cooperative: every block loops over 32 x 32 tiles. Phase 1 stages psi
+// on the tile plus halo (from the solver's split layout) and writes u, v and the row-major psi
+// of the tile. A bounded grid barrier follows (continuity reads u and v of neighbouring tiles);
+// phase 2 stages u and v on the tile plus halo and reduces DX u + DY v to max and min. The
+// reduction keeps, among equal values, the one with the smallest row-major index, which is
+// what the reference's sequential maxel/minel keep (so the sign of a zero extremum matches
+// too). The last block to finish folds the blocks' partials and writes the step record.
 #include <cfloat>
+#include <climits>
 
 #include "cnv_kernels.h"
 #include "cnv_stencil.cuh"
+#include "cnv_sync.cuh"
 
 namespace cnv {
 namespace {
+
+constexpr int kTX = 32;                 // tile columns (one warp across)
+constexpr int kTY = 32;                 // tile rows
+constexpr int kR = 3;                   // stencil radius (order 6; orders 2 and 4 use less)
+constexpr int kSW = kTX + 2 * kR;       // staged row width
+constexpr int kSH = kTY + 2 * kR;       // staged rows
+constexpr int kStepThreads = 256;       // 32 x 8: each thread takes 4 cells of one column
+constexpr int kRowsPerThread = kTY / (kStepThreads / kTX);
+constexpr int kBandDoubles = (int)(sizeof(FdBands) / sizeof(double));
 
 __device__ __forceinline__ double make_rhs(double f_ref, const StepArgs& a) {
     // src/poisson.c:247 multiplies dx*dx*dy*dy*f left to right: (((dx*dx)*dy)*dy)*f = c4*f
@@ -28,103 +57,191 @@ __device__ __forceinline__ double make_rhs(double f_ref, const StepArgs& a) {
     return g;
 }
 
-// ---------------------------------------------------------------------------- wall pass
-__global__ void k_wall(StepArgs a) {
-    if (a.ctrl->abort) return;
+// the operator bands, staged in shared memory by the whole block
+__device__ __forceinline__ void stage_bands(FdBands& sb, const FdBands* gb) {
+    double* d = reinterpret_cast<double*>(&sb);
+    const double* s = reinterpret_cast<const double*>(gb);
+    for (int x = threadIdx.x; x < kBandDoubles; x += blockDim.x) d[x] = __ldg(s + x);
+}
+
+// w at edge cell (i, j) after the wall loops of src/main.c:311-320: DX v - DY u with the
+// velocities' Dirichlet values (the corners get the same formula from both loops)
+__device__ __forceinline__ double wall_value(const StepArgs& a, const FdBands& b, int i, int j) {
     const int n = a.n;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= 4 * n) return;
-    const int side = s / n, t = s - side * n;
-    const int i = side == 0 ? 0 : side == 1 ? n - 1 : t;
-    const int j = side == 2 ? 0 : side == 3 ? n - 1 : t;
     const BoundaryValues bc = a.bc;
     const double* u = a.u;
     const double* v = a.v;
     auto U = [&](int r, int c) { return vel_bc(u, n, r, c, bc.u1, bc.u2, bc.u3, bc.u4); };
     auto V = [&](int r, int c) { return vel_bc(v, n, r, c, bc.v1, bc.v2, bc.v3, bc.v4); };
-    const double dvdx = along_j(a.bands->d1x, n, i, j, V);  // DX v
-    const double dudy = along_i(a.bands->d1y, n, i, j, U);  // DY u
-    a.w_wall[(size_t)i * n + j] = dsub(dvdx, dudy);
+    const double dvdx = along_j(b.d1x, n, i, j, V);  // DX v
+    const double dudy = along_i(b.d1y, n, i, j, U);  // DY u
+    return dsub(dvdx, dudy);
 }
 
-// ----------------------------------------------------------------------- transport pass
-__global__ void k_transport(StepArgs a) {
+__device__ __forceinline__ bool on_edge(int i, int j, int n) { return i == 0 || i == n - 1 || j == 0 || j == n - 1; }
+
+// ----------------------------------------------------------------------------------- k_pre
+__global__ void __launch_bounds__(kStepThreads) k_pre(StepArgs a) {
     if (a.ctrl->abort) return;
+    __shared__ double sw[kSH * kSW];
+    __shared__ FdBands sb;
     const int n = a.n;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= n || j >= n) return;
-    const double* w = a.w_in;
-    auto W = [&](int r, int c) { return w[(size_t)r * n + c]; };
-    const double wx = along_j(a.bands->d1x, n, i, j, W);   // dwdx   = DX  w
-    const double wy = along_i(a.bands->d1y, n, i, j, W);   // dwdy   = DY  w
-    const double wxx = along_j(a.bands->d2x, n, i, j, W);  // d2wdx2 = DX2 w
-    const double wyy = along_i(a.bands->d2y, n, i, j, W);  // d2wdy2 = DY2 w
+    const int j0 = blockIdx.x * kTX, i0 = blockIdx.y * kTY;
+    stage_bands(sb, a.bands);
+    __syncthreads();
+    // w on the tile and halo; edge cells take the wall value
+    const double* __restrict__ w = a.w_in;
+    for (int x = threadIdx.x; x < kSH * kSW; x += kStepThreads) {
+        const int r = x / kSW, c = x - r * kSW;
+        const int i = i0 - kR + r, j = j0 - kR + c;
+        double val = 0.0;
+        if (i >= 0 && i < n && j >= 0 && j < n) val = on_edge(i, j, n) ? wall_value(a, sb, i, j) : w[(size_t)i * n + j];
+        sw[x] = val;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+    const int j = j0 + tx;
+    if (j >= n) return;
+    auto W = [&](int r, int c) { return sw[(r - i0 + kR) * kSW + (c - j0 + kR)]; };
     const BoundaryValues bc = a.bc;
-    const double ue = vel_bc(a.u, n, i, j, bc.u1, bc.u2, bc.u3, bc.u4);
-    const double ve = vel_bc(a.v, n, i, j, bc.v1, bc.v2, bc.v3, bc.v4);
-    const double w0 = w[(size_t)i * n + j];
-    // (-u*dwdx - v*dwdy + (1./Re)*(d2wdx2 + d2wdy2))*dt + w   (src/fluiddyn.c:98)
-    const double conv = dsub(dmul(-ue, wx), dmul(ve, wy));
-    const double diff = dmul(a.inv_re, dadd(wxx, wyy));
-    const double wn = dadd(dmul(dadd(conv, diff), a.dt), w0);
-    a.w_out[(size_t)i * n + j] = wn;
-    if (a.rhs[0] && i > 0 && i < n - 1 && j > 0 && j < n - 1) {  // no rhs: direct solve reads w_out
-        const int c = (i + j) & 1;
-        a.rhs[c][(size_t)i * a.pitch + (j >> 1)] = make_rhs(-wn, a);  // f = -w (invsig)
+#pragma unroll 1
+    for (int k = 0; k < kRowsPerThread; ++k) {
+        const int i = i0 + ty + k * (kStepThreads / kTX);
+        if (i >= n) break;
+        const double wx = along_j(sb.d1x, n, i, j, W);   // dwdx   = DX  w
+        const double wy = along_i(sb.d1y, n, i, j, W);   // dwdy   = DY  w
+        const double wxx = along_j(sb.d2x, n, i, j, W);  // d2wdx2 = DX2 w
+        const double wyy = along_i(sb.d2y, n, i, j, W);  // d2wdy2 = DY2 w
+        const double ue = vel_bc(a.u, n, i, j, bc.u1, bc.u2, bc.u3, bc.u4);
+        const double ve = vel_bc(a.v, n, i, j, bc.v1, bc.v2, bc.v3, bc.v4);
+        const double w0 = W(i, j);
+        // (-u*dwdx - v*dwdy + (1./Re)*(d2wdx2 + d2wdy2))*dt + w   (src/fluiddyn.c:98)
+        const double conv = dsub(dmul(-ue, wx), dmul(ve, wy));
+        const double diff = dmul(a.inv_re, dadd(wxx, wyy));
+        const double wn = dadd(dmul(dadd(conv, diff), a.dt), w0);
+        const size_t at = (size_t)i * n + j;
+        a.w_out[at] = wn;
+        if (on_edge(i, j, n)) {
+            a.w_wall[at] = w0;  // the wall value, in place (src/main.c:311-320)
+        } else if (a.rhs[0]) {  // no rhs: the direct solve reads w_out itself
+            a.rhs[(i + j) & 1][(size_t)i * a.pitch + (j >> 1)] = make_rhs(-wn, a);  // f = -w (invsig)
+        }
     }
 }
 
-// ------------------------------------------------------------------------ velocity pass
-__global__ void k_velocity(StepArgs a) {
-    if (a.ctrl->abort) return;
+// ---------------------------------------------------------------------------------- k_post
+// Extremum with the reference's tie rule: among equal values the earliest (row-major) index.
+struct Ext {
+    double v;
+    int at;  // row-major index; -1 for the start value (which every tie keeps)
+};
+
+__device__ __forceinline__ void take_max(Ext& a, double v, int at) {
+    if (v > a.v || (v == a.v && at < a.at)) a = Ext{v, at};
+}
+__device__ __forceinline__ void take_min(Ext& a, double v, int at) {
+    if (v < a.v || (v == a.v && at < a.at)) a = Ext{v, at};
+}
+
+__device__ __forceinline__ void warp_ext(Ext& mx, Ext& mn) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double xv = __shfl_xor_sync(0xffffffffu, mx.v, off);
+        const int xa = __shfl_xor_sync(0xffffffffu, mx.at, off);
+        const double nv = __shfl_xor_sync(0xffffffffu, mn.v, off);
+        const int na = __shfl_xor_sync(0xffffffffu, mn.at, off);
+        take_max(mx, xv, xa);
+        take_min(mn, nv, na);
+    }
+}
+
+__global__ void __launch_bounds__(kStepThreads) k_post(StepArgs a, int continuity) {
+    if (a.ctrl->abort) return;  // stable for the whole launch: every block returns, or none
+    __shared__ double sm[2 * kSH * kSW];  // phase 1: psi; phase 2: u and v
+    __shared__ FdBands sb;
+    __shared__ int s_ok;
     const int n = a.n;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= n || j >= n) return;
+    const int tiles_x = (n + kTX - 1) / kTX;
+    const int tiles = tiles_x * ((n + kTY - 1) / kTY);
+    const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
+    stage_bands(sb, a.bands);
+    __syncthreads();
+
+    // phase 1: u = DY psi, v = -(DX psi), psi row-major
     const double* r = a.sor[0];
     const double* b = a.sor[1];
     const int pitch = a.pitch;
-    auto P = [&](int y, int x) { return ((y + x) & 1 ? b : r)[(size_t)y * pitch + (x >> 1)]; };
-    const double uu = along_i(a.bands->d1y, n, i, j, P);   // DY psi
-    const double vv = -along_j(a.bands->d1x, n, i, j, P);  // -(DX psi)
-    const size_t k = (size_t)i * n + j;
-    a.u[k] = uu;
-    a.v[k] = vv;
-    a.psi[k] = P(i, j);
-}
-
-// ---------------------------------------------------------------------- continuity pass
-constexpr int kContThreads = 256;
-
-__device__ __forceinline__ double gmax(double a, double b) { return b > a ? b : a; }
-__device__ __forceinline__ double gmin(double a, double b) { return b < a ? b : a; }
-
-__global__ void __launch_bounds__(kContThreads) k_continuity(StepArgs a) {
-    if (a.ctrl->abort) return;
-    const int n = a.n;
-    const long long total = (long long)n * n;
-    double mx = -DBL_MAX, mn = DBL_MAX;  // maxel/minel start values, src/linearalg.c:478, :514
-    const double* u = a.u;
-    const double* v = a.v;
-    auto U = [&](int r, int c) { return u[(size_t)r * n + c]; };
-    auto V = [&](int r, int c) { return v[(size_t)r * n + c]; };
-    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < total;
-         k += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(k / n), j = (int)(k - (long long)i * n);
-        const double dudx = along_j(a.bands->d1x, n, i, j, U);
-        const double dvdy = along_i(a.bands->d1y, n, i, j, V);
-        const double c = dadd(dudx, dvdy);
-        mx = gmax(mx, c);
-        mn = gmin(mn, c);
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int j0 = (tile % tiles_x) * kTX, i0 = (tile / tiles_x) * kTY;
+        for (int x = threadIdx.x; x < kSH * kSW; x += kStepThreads) {
+            const int rr = x / kSW, c = x - rr * kSW;
+            const int i = i0 - kR + rr, j = j0 - kR + c;
+            sm[x] = (i >= 0 && i < n && j >= 0 && j < n) ? ((i + j) & 1 ? b : r)[(size_t)i * pitch + (j >> 1)] : 0.0;
+        }
+        __syncthreads();
+        auto P = [&](int y, int c) { return sm[(y - i0 + kR) * kSW + (c - j0 + kR)]; };
+        const int j = j0 + tx;
+        if (j < n) {
+#pragma unroll 1
+            for (int k = 0; k < kRowsPerThread; ++k) {
+                const int i = i0 + ty + k * (kStepThreads / kTX);
+                if (i >= n) break;
+                const double uu = along_i(sb.d1y, n, i, j, P);   // DY psi
+                const double vv = -along_j(sb.d1x, n, i, j, P);  // -(DX psi)
+                const size_t at = (size_t)i * n + j;
+                a.u[at] = uu;
+                a.v[at] = vv;
+                a.psi[at] = P(i, j);
+            }
+        }
+        __syncthreads();
     }
-    __shared__ double smx[kContThreads / 32], smn[kContThreads / 32];
+    if (!continuity) return;
+
+    // bounded grid barrier: continuity reads the neighbouring tiles' u and v
+    Ctrl* ctl = a.ctrl;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&ctl->bar_count, 1u);
+        s_ok = wait_geq(&ctl->bar_count, gridDim.x, ctl, a.timeout_ns) ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_ok) return;  // timeout (status recorded) or another block's abort
+
+    // phase 2: continuity DX u + DY v (the raw velocities the reference's continuity() reads)
+    Ext mx{-DBL_MAX, -1}, mn{DBL_MAX, -1};  // maxel/minel start values, src/linearalg.c:478, :514
+    double* su = sm;
+    double* sv = sm + kSH * kSW;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int j0 = (tile % tiles_x) * kTX, i0 = (tile / tiles_x) * kTY;
+        for (int x = threadIdx.x; x < kSH * kSW; x += kStepThreads) {
+            const int rr = x / kSW, c = x - rr * kSW;
+            const int i = i0 - kR + rr, j = j0 - kR + c;
+            const bool in = i >= 0 && i < n && j >= 0 && j < n;
+            su[x] = in ? __ldcg(a.u + (size_t)i * n + j) : 0.0;  // written by other blocks: via L2
+            sv[x] = in ? __ldcg(a.v + (size_t)i * n + j) : 0.0;
+        }
+        __syncthreads();
+        auto U = [&](int y, int c) { return su[(y - i0 + kR) * kSW + (c - j0 + kR)]; };
+        auto V = [&](int y, int c) { return sv[(y - i0 + kR) * kSW + (c - j0 + kR)]; };
+        const int j = j0 + tx;
+        if (j < n) {
+#pragma unroll 1
+            for (int k = 0; k < kRowsPerThread; ++k) {
+                const int i = i0 + ty + k * (kStepThreads / kTX);
+                if (i >= n) break;
+                const double dudx = along_j(sb.d1x, n, i, j, U);
+                const double dvdy = along_i(sb.d1y, n, i, j, V);
+                const double c = dadd(dudx, dvdy);
+                take_max(mx, c, i * n + j);
+                take_min(mn, c, i * n + j);
+            }
+        }
+        __syncthreads();
+    }
+    __shared__ Ext smx[kStepThreads / 32], smn[kStepThreads / 32];
     __shared__ bool last;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        mx = gmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
-        mn = gmin(mn, __shfl_xor_sync(0xffffffffu, mn, off));
-    }
+    warp_ext(mx, mn);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) {
         smx[warp] = mx;
@@ -132,37 +249,40 @@ __global__ void __launch_bounds__(kContThreads) k_continuity(StepArgs a) {
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < kContThreads / 32; ++w) {
-            mx = gmax(mx, smx[w]);
-            mn = gmin(mn, smn[w]);
+        for (int w = 1; w < kStepThreads / 32; ++w) {
+            take_max(mx, smx[w].v, smx[w].at);
+            take_min(mn, smn[w].v, smn[w].at);
         }
-        a.cont_partials[2 * blockIdx.x] = mx;
-        a.cont_partials[2 * blockIdx.x + 1] = mn;
+        double* part = a.cont_partials + 4 * blockIdx.x;
+        part[0] = mx.v;
+        part[1] = (double)mx.at;
+        part[2] = mn.v;
+        part[3] = (double)mn.at;
         __threadfence();
-        const unsigned t = atomicAdd(&a.ctrl->cont_ticket, 1u);
+        const unsigned t = atomicAdd(&ctl->cont_ticket, 1u);
         last = (t == gridDim.x - 1);
     }
     __syncthreads();
     if (!last || threadIdx.x != 0) return;
-    // last block: fold the partials, write this step's record
+    // last block: fold the partials, write this step's record, re-arm the barrier and ticket
     __threadfence();
     const volatile double* cp = a.cont_partials;
-    mx = -DBL_MAX;
-    mn = DBL_MAX;
-    for (int b = 0; b < (int)gridDim.x; ++b) {
-        mx = gmax(mx, cp[2 * b]);
-        mn = gmin(mn, cp[2 * b + 1]);
+    mx = Ext{-DBL_MAX, -1};
+    mn = Ext{DBL_MAX, -1};
+    for (int q = 0; q < (int)gridDim.x; ++q) {
+        take_max(mx, cp[4 * q], (int)cp[4 * q + 1]);
+        take_min(mn, cp[4 * q + 2], (int)cp[4 * q + 3]);
     }
-    Ctrl* ctl = a.ctrl;
     ctl->cont_ticket = 0;
+    ctl->bar_count = 0;  // every block passed the barrier before taking its ticket
     const int step = ctl->step;
     if (step < ctl->max_records) {
-        StepRecord& r = ctl->records[step];
-        r.iters = ctl->iters;
-        r.status = ctl->status;
-        r.err = ctl->err;
-        r.cont_max = mx;
-        r.cont_min = mn;
+        StepRecord& rec = ctl->records[step];
+        rec.iters = ctl->iters;
+        rec.status = ctl->status;
+        rec.err = ctl->err;
+        rec.cont_max = mx.v;
+        rec.cont_min = mn.v;
     }
     ctl->step = step + 1;
 }
@@ -194,29 +314,44 @@ __global__ void k_nonfinite(const double* x, long long count, int* flag) {
 
 dim3 grid2d(int n, dim3 blk) { return dim3((n + blk.x - 1) / blk.x, (n + blk.y - 1) / blk.y); }
 
+int tile_count(int n) { return ((n + kTX - 1) / kTX) * ((n + kTY - 1) / kTY); }
+
 }  // namespace
 
-cudaError_t launch_wall(const StepArgs& a, cudaStream_t s) {
-    const int threads = 128;
-    k_wall<<<(4 * a.n + threads - 1) / threads, threads, 0, s>>>(a);
+cudaError_t launch_pre(const StepArgs& a, cudaStream_t s) {
+    k_pre<<<dim3((a.n + kTX - 1) / kTX, (a.n + kTY - 1) / kTY), kStepThreads, 0, s>>>(a);
     return cudaGetLastError();
 }
 
-cudaError_t launch_transport(const StepArgs& a, cudaStream_t s) {
-    const dim3 blk(32, 8);
-    k_transport<<<grid2d(a.n, blk), blk, 0, s>>>(a);
-    return cudaGetLastError();
+int post_grid(int n, int device) {
+    int sms = 0, per_sm = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_post, kStepThreads, 0) != cudaSuccess || per_sm < 1)
+        return 0;
+    const int tiles = tile_count(n);
+    return tiles < sms * per_sm ? tiles : sms * per_sm;
 }
 
-cudaError_t launch_velocity(const StepArgs& a, cudaStream_t s) {
-    const dim3 blk(32, 8);
-    k_velocity<<<grid2d(a.n, blk), blk, 0, s>>>(a);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_continuity(const StepArgs& a, cudaStream_t s) {
-    k_continuity<<<a.cont_blocks, kContThreads, 0, s>>>(a);
-    return cudaGetLastError();
+cudaError_t launch_post(const StepArgs& a, bool continuity, cudaStream_t s) {
+    int c = continuity ? 1 : 0;
+    if (!continuity) {  // no barrier: one block per tile
+        k_post<<<tile_count(a.n), kStepThreads, 0, s>>>(a, c);
+        return cudaGetLastError();
+    }
+    // the grid barrier needs every block resident: a cooperative launch of at most post_grid blocks
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(a.cont_blocks);
+    cfg.blockDim = dim3(kStepThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    StepArgs args = a;
+    void* kargs[] = {&args, &c};
+    return cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_post), kargs);
 }
 
 cudaError_t launch_to_split(const double* f, double* r, double* b, const StepArgs& a, cudaStream_t s) {
