@@ -5,21 +5,36 @@
 //
 //     den psi(i,j) - dy^2 (psi(i+1,j) + psi(i-1,j)) - dx^2 (psi(i,j+1) + psi(i,j-1)) = c4 w(i,j)
 //
-// (den = 2 (dx^2 + dy^2), c4 = dx^2 dy^2, f = -w). Its matrix M is the Kronecker sum of two
+// (den = 2 (dx^2 + dy^2), c4 = dx^2 dy^2, f = -w). Its matrix is the Kronecker sum of two
 // tridiagonal Toeplitz matrices, diagonalised by the orthonormal DST-I basis
 //     S[a][b] = sqrt(2 / (m+1)) sin(pi (a+1)(b+1) / (m+1)),  m = n - 2,  S = S^T = S^-1,
-// with eigenvalues den - 2 dy^2 cos(pi (a+1)/(m+1)) - 2 dx^2 cos(pi (b+1)/(m+1)). So
-//     psi = S ((S (c4 w) S) ./ Lambda) S,
-// four m x m products in FP64 and one division per cell: the converged answer of the
-// reference's solver to rounding, at a fixed cost, and an exactly linear, symmetric map (the
-// adjoint solve is the same call). This is what the differentiable form uses: a finite-
-// difference check of the gradient needs a solve far tighter than an iterative stop rule gives.
+// with eigenvalues lambda(a, b) = 4 dy^2 sin^2(t_a / 2) + 4 dx^2 sin^2(t_b / 2), t_k = pi (k+1)/(m+1).
+// With X the interior of psi as an m x m matrix (rows i) and R = c4 w:  X = S ((S R S) ./ lambda) S,
+// done as four row transforms (each pass transforms every row of its input):
+//     1. along j, written transposed      (rows: j-modes b, over i)
+//     2. along i, divided by lambda        (rows: b, over i-modes a)
+//     3. along a (inverse), written transposed (rows: i, over b)
+//     4. along b (inverse), into psi
+// The eigenvalues are formed as sums of squared sines, not as den - 2 dy^2 cos - 2 dx^2 cos: that
+// difference cancels in the lowest modes (at n = 1024 it loses about four digits), while the
+// transforms themselves are orthogonal, so the solve is accurate to a few units of rounding
+// (measured against an extended-precision solve). The answer is what the reference's solver
+// converges to, to rounding, at a fixed cost; the map is linear and symmetric, so the adjoint
+// solve is the same call. The differentiable form uses it: a finite-difference check of the
+// gradient needs a solve far tighter than an iterative stop rule gives.
 //
-// Each product uses the mirror symmetry S[m-1-a][b] = (-1)^b S[a][b]: for a < ceil(m/2) the
-// kernels accumulate the even-b and odd-b halves of the dot product separately (E, O) and write
-// E + O to row a and E - O to row m-1-a, halving the FP64 work (m^3 / 2 fused multiply-adds per
-// product). FP64 arithmetic bounds these kernels (GB300's FP64 rate is low); operands are
-// staged in shared memory tiles.
+// The row transforms. A DST-I of length m is the DFT of length len = 2(m+1) of
+// the row's odd extension (0, x_0 .. x_{m-1}, 0, -x_{m-1} .. -x_0): the DFT is -2i times the
+// unnormalised DST. Two rows go into one complex sequence (row a as its real part, row b as its
+// imaginary part); the DFT of that sequence is -2i DST(a) + 2 DST(b), so one complex FFT gives
+// both rows. The FFT is a mixed-radix Stockham transform (self-sorting, two shared-memory
+// buffers, one block per row pair) over the prime factors p of len: each stage applies the
+// twiddles, then a p-point DFT in its symmetric form (for odd p, outputs q and p-q share the
+// sums over u_q + u_{p-q} and u_q - u_{p-q}: 2(p-1) multiply-adds per output pair). Per row
+// that is about len * (sum of the radices) multiply-adds, against m^2 / 2 for a dense product:
+// at n = 1024 (len = 2046 = 2 * 3 * 11 * 31) about 10 times fewer FP64 operations. Grids whose
+// len has a prime factor above kMaxRadix, or that do not fit shared memory, take the dense
+// products with S instead (each folded by the mirror symmetry S[b][m-1-c] = (-1)^b S[b][c]).
 #include <cmath>
 #include <vector>
 
@@ -28,82 +43,172 @@
 namespace cnv {
 namespace {
 
-constexpr int kCols = 64;     // output columns per block (one per thread column)
-constexpr int kRowsT = 4;     // thread rows per block
-constexpr int kBk = 32;       // reduction chunk (even, so chunk-local parity = global parity)
-constexpr int kThreads = kCols * kRowsT;
+// ---------------------------------------------------------------- FFT row transforms
+constexpr int kFftThreads = 512;
 
-// out = S * X (left product). X(b, c) = xs * x[(b + xo) * xld + c + xo]. Row a < half of the
-// block's folded rows gets E + O, row m-1-a gets E - O. RA folded rows per block (multiple of 4).
-template <int RA>
-__global__ void __launch_bounds__(kThreads) k_dst_left(const double* __restrict__ S, int m,
-                                                       const double* __restrict__ x, int xld, int xo, double xs,
-                                                       double* __restrict__ out, int old, int oo) {
-    __shared__ double s_s[RA][kBk + 1];
-    __shared__ double s_x[kBk][kCols];
-    const int half = (m + 1) / 2;
-    const int tx = threadIdx.x % kCols, ty = threadIdx.x / kCols;
-    const int a0 = blockIdx.y * RA, c = blockIdx.x * kCols + tx;
-    constexpr int Q = RA / kRowsT;
-    double e[Q], o[Q];
-#pragma unroll
-    for (int q = 0; q < Q; ++q) e[q] = o[q] = 0.0;
-    for (int b0 = 0; b0 < m; b0 += kBk) {
-        for (int t = threadIdx.x; t < RA * kBk; t += kThreads) {
-            const int r = t / kBk, bb = t % kBk;
-            const int a = a0 + r, b = b0 + bb;
-            s_s[r][bb] = (a < half && b < m) ? S[(size_t)a * m + b] : 0.0;
-        }
-        for (int t = threadIdx.x; t < kBk * kCols; t += kThreads) {
-            const int bb = t / kCols, cc = t % kCols;
-            const int b = b0 + bb, col = blockIdx.x * kCols + cc;
-            s_x[bb][cc] = (b < m && col < m) ? xs * x[(size_t)(b + xo) * xld + col + xo] : 0.0;
-        }
-        __syncthreads();
-#pragma unroll 8
-        for (int bb = 0; bb < kBk; bb += 2) {
-            const double xe = s_x[bb][tx], xodd = s_x[bb + 1][tx];
-#pragma unroll
-            for (int q = 0; q < Q; ++q) {
-                e[q] = __fma_rn(s_s[ty + kRowsT * q][bb], xe, e[q]);
-                o[q] = __fma_rn(s_s[ty + kRowsT * q][bb + 1], xodd, o[q]);
-            }
-        }
-        __syncthreads();
-    }
-    if (c >= m) return;
-#pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        const int a = a0 + ty + kRowsT * q;
-        if (a >= half) continue;
-        out[(size_t)(a + oo) * old + c + oo] = e[q] + o[q];
-        if (m - 1 - a != a) out[(size_t)(m - 1 - a + oo) * old + c + oo] = e[q] - o[q];
-    }
-}
+struct FftArgs {
+    int m, len, nstages;
+    int radix[kMaxFftStages];
+    int csoff[kMaxFftStages];  // offset of each stage's p-point table in cs
+    int ncs;
+    const double2* tw;         // exp(-2 pi i t / len), t = 0 .. len-1
+    const double2* cs;         // per stage: (cos 2 pi t / p, sin 2 pi t / p), t = 0 .. p-1
+    double norm;               // 1 / sqrt(2 (m+1)): orthonormal DST from the DFT
+};
 
-// Destination of a right product: row-major out[(r + off) * ld + c + off], or, when red is
-// set, the red/black split layout of an n x n field (cell (i, j) = (r + off, c + off) at
-// (i + j odd ? black : red)[i * pitch + j / 2]).
+// Destination of a transform's value for row r, column c: row-major out[(r + off) * ld + c + off],
+// or out[c * ld + r] when transposed, or, when red is set, the red/black split layout of an n x n
+// field (cell (i, j) = (r + off, c + off) at (i + j odd ? black : red)[i * pitch + j / 2]). With
+// lam_r set, the value is first divided by lam_r[r] + lam_c[c].
 struct DstDest {
     double* out;
     int ld, off;
     double* red;
     double* black;
     int pitch;
+    int transposed;
+    const double* lam_r;
+    const double* lam_c;
     __device__ __forceinline__ void put(int r, int c, double val) const {
+        if (lam_r) val = val / (__ldg(lam_r + r) + __ldg(lam_c + c));
+        if (transposed) {
+            out[(size_t)c * ld + r] = val;
+            return;
+        }
         const int i = r + off, j = c + off;
         if (red) ((i + j) & 1 ? black : red)[(size_t)i * pitch + (j >> 1)] = val;
         else out[(size_t)i * ld + j] = val;
     }
 };
 
-// out = X * S (right product), optionally divided by the eigenvalues. X(r, b) = x[r * xld + b]
-// (m x m scratch). Column c < half gets E + O, column m-1-c gets E - O. RR rows per block.
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+    return make_double2(__fma_rn(a.x, b.x, -a.y * b.y), __fma_rn(a.x, b.y, a.y * b.x));
+}
+
+// Orthonormal DST-I of rows 2*blockIdx.x and 2*blockIdx.x + 1 of X(r, c) = xs * x[(r + xo) * xld
+// + c + xo] (r, c < m), written to dst.
+__global__ void __launch_bounds__(kFftThreads) k_dst_fft(FftArgs F, const double* __restrict__ x, int xld, int xo,
+                                                          double xs, DstDest dst) {
+    extern __shared__ double2 fsm[];
+    double2* X = fsm;               // the sequence between stages
+    double2* T = fsm + F.len;       // a stage's twiddled (and for odd p, paired) inputs
+    double2* CS = fsm + 2 * F.len;  // the stages' p-point tables
+    const int m = F.m, len = F.len;
+    const int ra = 2 * blockIdx.x, rb = ra + 1;  // rb == m: no second row
+    for (int t = threadIdx.x; t < F.ncs; t += kFftThreads) CS[t] = F.cs[t];
+    const double* xa = x + (size_t)(ra + xo) * xld + xo;
+    const double* xb = x + (size_t)(rb + xo) * xld + xo;
+    for (int t = threadIdx.x; t < len; t += kFftThreads) {
+        // odd extension: 0, x_0 .. x_{m-1}, 0, -x_{m-1} .. -x_0
+        double a = 0.0, b = 0.0;
+        if (t != 0 && t != m + 1) {
+            const bool lo = t <= m;
+            const int c = lo ? t - 1 : len - t - 1;
+            a = xs * __ldg(xa + c);
+            b = rb < m ? xs * __ldg(xb + c) : 0.0;
+            if (!lo) {
+                a = -a;
+                b = -b;
+            }
+        }
+        X[t] = make_double2(a, b);
+    }
+    __syncthreads();
+    int L = 1;  // length of the sub-transforms done so far
+    for (int s = 0; s < F.nstages; ++s) {
+        const int p = F.radix[s];
+        const int Lp = L * p, r2 = len / Lp, nb = len / p;  // nb butterflies of p points
+        const int stride = r2 * L;                           // between a butterfly's inputs
+        const double2* cs = CS + F.csoff[s];
+        if (p == 2) {
+            for (int b = threadIdx.x; b < nb; b += kFftThreads) {
+                const int k = b / L, j1 = b - k * L;
+                const double2 u0 = X[k * L + j1];
+                const double2 u1 = cmul(X[k * L + j1 + stride], __ldg(F.tw + j1 * r2));
+                T[2 * b] = make_double2(u0.x + u1.x, u0.y + u1.y);
+                T[2 * b + 1] = make_double2(u0.x - u1.x, u0.y - u1.y);
+            }
+            __syncthreads();
+            for (int e = threadIdx.x; e < len; e += kFftThreads) {
+                const int b = e >> 1, q2 = e & 1;
+                const int k = b / L, j1 = b - k * L;
+                X[k * Lp + j1 + L * q2] = T[e];
+            }
+            __syncthreads();
+        } else {
+            const int h = (p - 1) / 2;
+            const int per = h + 1;
+            // twiddled inputs: u_0, and A_q = u_q + u_{p-q}, B_q = u_q - u_{p-q} (q = 1 .. h)
+            for (int e = threadIdx.x; e < nb * per; e += kFftThreads) {
+                const int b = e / per, q = e - b * per;
+                const int k = b / L, j1 = b - k * L;
+                const int base = k * L + j1;
+                if (q == 0) {
+                    T[b * p] = X[base];
+                } else {
+                    const double2 uq = cmul(X[base + q * stride], __ldg(F.tw + q * j1 * r2));
+                    const double2 up = cmul(X[base + (p - q) * stride], __ldg(F.tw + (p - q) * j1 * r2));
+                    T[b * p + q] = make_double2(uq.x + up.x, uq.y + up.y);
+                    T[b * p + h + q] = make_double2(uq.x - up.x, uq.y - up.y);
+                }
+            }
+            __syncthreads();
+            // outputs q2 and p - q2 of each butterfly: u_0 + C -+ i D with
+            // C = sum_q A_q cos(2 pi q q2 / p), D = sum_q B_q sin(2 pi q q2 / p)
+            for (int e = threadIdx.x; e < nb * per; e += kFftThreads) {
+                const int b = e / per, q2 = e - b * per;
+                const int k = b / L, j1 = b - k * L;
+                const int ob = k * Lp + j1;
+                const double2* tb = T + b * p;
+                const double2 u0 = tb[0];
+                if (q2 == 0) {
+                    double2 acc = u0;
+                    for (int q = 1; q <= h; ++q) {
+                        acc.x += tb[q].x;
+                        acc.y += tb[q].y;
+                    }
+                    X[ob] = acc;
+                } else {
+                    double2 C = make_double2(0.0, 0.0), D = make_double2(0.0, 0.0);
+                    int t = 0;
+                    for (int q = 1; q <= h; ++q) {
+                        t += q2;
+                        if (t >= p) t -= p;
+                        const double2 w = cs[t];
+                        const double2 A = tb[q], B = tb[h + q];
+                        C.x = __fma_rn(A.x, w.x, C.x);
+                        C.y = __fma_rn(A.y, w.x, C.y);
+                        D.x = __fma_rn(B.x, w.y, D.x);
+                        D.y = __fma_rn(B.y, w.y, D.y);
+                    }
+                    X[ob + L * q2] = make_double2(u0.x + C.x + D.y, u0.y + C.y - D.x);
+                    X[ob + L * (p - q2)] = make_double2(u0.x + C.x - D.y, u0.y + C.y + D.x);
+                }
+            }
+            __syncthreads();
+        }
+        L = Lp;
+    }
+    // bins 1 .. m: DFT = -2i DST(a) + 2 DST(b)
+    for (int k = 1 + threadIdx.x; k <= m; k += kFftThreads) {
+        const double2 W = X[k];
+        dst.put(ra, k - 1, -W.y * F.norm);
+        if (rb < m) dst.put(rb, k - 1, W.x * F.norm);
+    }
+}
+
+// ------------------------------------------------------- dense fallback: out = X * S
+constexpr int kCols = 64;     // output columns per block (one per thread column)
+constexpr int kRowsT = 4;     // thread rows per block
+constexpr int kBk = 32;       // reduction chunk (even, so chunk-local parity = global parity)
+constexpr int kThreads = kCols * kRowsT;
+
+// X(r, b) = xs * x[(r + xo) * xld + b + xo]. Column c < half gets E + O, column m-1-c gets E - O
+// (E, O: the even-b and odd-b halves of the dot product). RR rows per block.
 template <int RR>
 __global__ void __launch_bounds__(kThreads) k_dst_right(const double* __restrict__ S, int m,
-                                                        const double* __restrict__ x, int xld, DstDest dst,
-                                                        const double* __restrict__ li,
-                                                        const double* __restrict__ lj, double den) {
+                                                        const double* __restrict__ x, int xld, int xo, double xs,
+                                                        DstDest dst) {
     __shared__ double s_x[RR][kBk + 1];
     __shared__ double s_s[kBk][kCols];
     const int half = (m + 1) / 2;
@@ -117,7 +222,7 @@ __global__ void __launch_bounds__(kThreads) k_dst_right(const double* __restrict
         for (int t = threadIdx.x; t < RR * kBk; t += kThreads) {
             const int r = t / kBk, bb = t % kBk;
             const int row = r0 + r, b = b0 + bb;
-            s_x[r][bb] = (row < m && b < m) ? x[(size_t)row * xld + b] : 0.0;
+            s_x[r][bb] = (row < m && b < m) ? xs * x[(size_t)(row + xo) * xld + b + xo] : 0.0;
         }
         for (int t = threadIdx.x; t < kBk * kCols; t += kThreads) {
             const int bb = t / kCols, cc = t % kCols;
@@ -142,52 +247,74 @@ __global__ void __launch_bounds__(kThreads) k_dst_right(const double* __restrict
     for (int q = 0; q < Q; ++q) {
         const int r = r0 + ty + kRowsT * q;
         if (r >= m) continue;
-        double p = e[q] + o[q], n2 = e[q] - o[q];
-        if (li) {
-            p = p / (den - li[r] - lj[c]);
-            n2 = n2 / (den - li[r] - lj[c2]);
-        }
-        dst.put(r, c, p);
-        if (c2 != c) dst.put(r, c2, n2);
+        dst.put(r, c, e[q] + o[q]);
+        if (c2 != c) dst.put(r, c2, e[q] - o[q]);
     }
 }
 
 int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
-template <int R>
-cudaError_t left(const DstPlan& P, const double* x, int xld, int xo, double xs, double* out, int old, int oo,
-                 cudaStream_t s) {
-    const dim3 grid(ceil_div(P.m, kCols), ceil_div((P.m + 1) / 2, R));
-    k_dst_left<R><<<grid, kThreads, 0, s>>>(P.S, P.m, x, xld, xo, xs, out, old, oo);
-    return cudaGetLastError();
-}
-
-template <int R>
-cudaError_t right(const DstPlan& P, const double* x, const DstDest& d, bool divide, cudaStream_t s) {
-    const dim3 grid(ceil_div((P.m + 1) / 2, kCols), ceil_div(P.m, R));
-    k_dst_right<R><<<grid, kThreads, 0, s>>>(P.S, P.m, x, P.m, d, divide ? P.li : nullptr, divide ? P.lj : nullptr,
-                                            P.den);
-    return cudaGetLastError();
-}
-
-template <int R>
-cudaError_t solve(const DstPlan& P, const double* in, double scale, const DstDest& d, cudaStream_t s) {
-    // t1 = S (scale * in), t2 = (t1 S) ./ Lambda, t1 = S t2, out = t1 S
-    const int n = P.n, m = P.m;
-    const DstDest t2{P.t2, m, 0, nullptr, nullptr, 0};
-    cudaError_t e;
-    if ((e = left<R>(P, in, n, 1, scale, P.t1, m, 0, s)) != cudaSuccess) return e;
-    if ((e = right<R>(P, P.t1, t2, true, s)) != cudaSuccess) return e;
-    if ((e = left<R>(P, P.t2, m, 0, 1.0, P.t1, m, 0, s)) != cudaSuccess) return e;
-    return right<R>(P, P.t1, d, false, s);
-}
-
-cudaError_t solve_any(const DstPlan& P, const double* in, double scale, const DstDest& d, cudaStream_t s) {
-    switch (P.rows) {
-        case 16: return solve<16>(P, in, scale, d, s);
-        case 8: return solve<8>(P, in, scale, d, s);
-        default: return solve<4>(P, in, scale, d, s);
+FftArgs fft_args(const DstPlan& P) {
+    FftArgs F{};
+    F.m = P.m;
+    F.len = P.len;
+    F.nstages = P.nstages;
+    for (int s = 0; s < P.nstages; ++s) {
+        F.radix[s] = P.radix[s];
+        F.csoff[s] = P.csoff[s];
     }
+    F.ncs = P.ncs;
+    F.tw = P.tw;
+    F.cs = P.cs;
+    F.norm = 1.0 / std::sqrt(2.0 * (P.m + 1));
+    return F;
+}
+
+// One transform along j of every row: dst(r, c) = sum_b X(r, b) S[b][c], X(r, b) = xs *
+// x[(r + xo) * xld + b + xo].
+cudaError_t transform_rows(const DstPlan& P, const double* x, int xld, int xo, double xs, const DstDest& d,
+                           cudaStream_t s) {
+    if (P.len) {
+        k_dst_fft<<<ceil_div(P.m, 2), kFftThreads, P.fft_smem, s>>>(fft_args(P), x, xld, xo, xs, d);
+        return cudaGetLastError();
+    }
+    const dim3 grid(ceil_div((P.m + 1) / 2, kCols), ceil_div(P.m, P.rows));
+    switch (P.rows) {
+        case 16: k_dst_right<16><<<grid, kThreads, 0, s>>>(P.S, P.m, x, xld, xo, xs, d); break;
+        case 8: k_dst_right<8><<<grid, kThreads, 0, s>>>(P.S, P.m, x, xld, xo, xs, d); break;
+        default: k_dst_right<4><<<grid, kThreads, 0, s>>>(P.S, P.m, x, xld, xo, xs, d); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t solve(const DstPlan& P, const double* in, double scale, const DstDest& d, cudaStream_t s) {
+    const int m = P.m;
+    const DstDest t1_tr{P.t1, m, 0, nullptr, nullptr, 0, 1, nullptr, nullptr};
+    const DstDest t2_div{P.t2, m, 0, nullptr, nullptr, 0, 0, P.lam_j, P.lam_i};  // rows b, columns a
+    cudaError_t e;
+    if ((e = transform_rows(P, in, P.n, 1, scale, t1_tr, s)) != cudaSuccess) return e;  // along j
+    if ((e = transform_rows(P, P.t1, m, 0, 1.0, t2_div, s)) != cudaSuccess) return e;   // along i, / lambda
+    if ((e = transform_rows(P, P.t2, m, 0, 1.0, t1_tr, s)) != cudaSuccess) return e;    // back along a
+    return transform_rows(P, P.t1, m, 0, 1.0, d, s);                                     // back along b
+}
+
+// Prime factors of len (ascending), or false when one exceeds kMaxRadix or there are too many.
+bool factor(int len, int* radix, int* count) {
+    int c = 0;
+    for (int p = 2; len > 1; ++p) {
+        while (len % p == 0) {
+            if (p > kMaxRadix || c == kMaxFftStages) return false;
+            radix[c++] = p;
+            len /= p;
+        }
+        if (p * p > len && len > 1) {
+            if (len > kMaxRadix || c == kMaxFftStages) return false;
+            radix[c++] = len;
+            len = 1;
+        }
+    }
+    *count = c;
+    return true;
 }
 
 }  // namespace
@@ -199,39 +326,87 @@ int dst_plan_create(int n, double dx, double dy, DstPlan* P) {
     P->n = n;
     P->m = m;
     P->den = 2 * (dx * dx + dy * dy);
-    std::vector<double> S((size_t)m * m), li(m), lj(m);
+    P->dx2 = dx * dx;
+    P->dy2 = dy * dy;
     const double pi = std::acos(-1.0);
-    const double scale = std::sqrt(2.0 / (m + 1));
-    const long long period = 2LL * (m + 1);
-    for (int a = 0; a < m; ++a)
-        for (int b = 0; b < m; ++b) {
-            const long long k = ((long long)(a + 1) * (b + 1)) % period;  // exact argument reduction
-            S[(size_t)a * m + b] = scale * std::sin(pi * (double)k / (m + 1));
+    int dev = 0, smem_max = 0, sms = 148;
+    if (cudaGetDevice(&dev) != cudaSuccess) return CNV_CUDA_ERROR;
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+
+    // the FFT row transforms where len = 2(m+1) factors into small primes and fits shared memory
+    const int len = 2 * (m + 1);
+    int radix[kMaxFftStages], ns = 0;
+    if (factor(len, radix, &ns)) {
+        int ncs = 0;
+        for (int s = 0; s < ns; ++s) ncs += radix[s];
+        const size_t smem = (2 * (size_t)len + ncs) * sizeof(double2);
+        if (smem <= (size_t)smem_max) {
+            P->len = len;
+            P->nstages = ns;
+            P->ncs = ncs;
+            P->fft_smem = (int)smem;
+            std::vector<double2> tw(len), cs(ncs);
+            // tables in long double, rounded once to double
+            const long double lpi = 3.141592653589793238462643383279502884L;
+            for (int t = 0; t < len; ++t) {
+                const long double a = 2 * lpi * t / len;  // exp(-2 pi i t / len)
+                tw[t] = make_double2((double)std::cos(a), (double)-std::sin(a));
+            }
+            for (int s = 0, off = 0; s < ns; ++s) {
+                P->radix[s] = radix[s];
+                P->csoff[s] = off;
+                for (int t = 0; t < radix[s]; ++t) {
+                    const long double a = 2 * lpi * t / radix[s];
+                    cs[off + t] = make_double2((double)std::cos(a), (double)std::sin(a));
+                }
+                off += radix[s];
+            }
+            if (cudaMalloc(&P->tw, len * sizeof(double2)) != cudaSuccess ||
+                cudaMalloc(&P->cs, ncs * sizeof(double2)) != cudaSuccess ||
+                cudaMemcpy(P->tw, tw.data(), len * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemcpy(P->cs, cs.data(), ncs * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaFuncSetAttribute(k_dst_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, P->fft_smem) !=
+                    cudaSuccess) {
+                dst_plan_destroy(P);
+                return CNV_CUDA_ERROR;
+            }
         }
-    for (int a = 0; a < m; ++a) {
-        li[a] = 2 * dy * dy * std::cos(pi * (a + 1) / (m + 1));
-        lj[a] = 2 * dx * dx * std::cos(pi * (a + 1) / (m + 1));
+    }
+    if (!P->len) {
+        // dense products with the DST matrix
+        std::vector<double> S((size_t)m * m);
+        const double scale = std::sqrt(2.0 / (m + 1));
+        const long long period = 2LL * (m + 1);
+        for (int a = 0; a < m; ++a)
+            for (int b = 0; b < m; ++b) {
+                const long long k = ((long long)(a + 1) * (b + 1)) % period;  // exact argument reduction
+                S[(size_t)a * m + b] = scale * std::sin(pi * (double)k / (m + 1));
+            }
+        if (cudaMalloc(&P->S, (size_t)m * m * sizeof(double)) != cudaSuccess ||
+            cudaMemcpy(P->S, S.data(), (size_t)m * m * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+            dst_plan_destroy(P);
+            return CNV_CUDA_ERROR;
+        }
+        // more, smaller blocks when the grid is small, so that every SM gets work
+        const int cols = ceil_div((m + 1) / 2, kCols);
+        P->rows = (cols * ceil_div(m, 16) >= 2 * sms) ? 16 : (cols * ceil_div(m, 8) >= 2 * sms) ? 8 : 4;
+    }
+    // eigenvalue parts 4 h^2 sin^2(pi (k+1) / (2 (m+1))), in long double, rounded once
+    std::vector<double> li(m), lj(m);
+    for (int k = 0; k < m; ++k) {
+        const long double sk = std::sin(3.141592653589793238462643383279502884L * (k + 1) / (2.0L * (m + 1)));
+        li[k] = (double)(4.0L * (long double)P->dy2 * sk * sk);
+        lj[k] = (double)(4.0L * (long double)P->dx2 * sk * sk);
     }
     const size_t mm = (size_t)m * m;
-    if (cudaMalloc(&P->S, mm * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&P->t1, mm * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&P->t2, mm * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&P->li, m * sizeof(double)) != cudaSuccess ||
-        cudaMalloc(&P->lj, m * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&P->t1, mm * sizeof(double)) != cudaSuccess || cudaMalloc(&P->t2, mm * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&P->lam_i, m * sizeof(double)) != cudaSuccess || cudaMalloc(&P->lam_j, m * sizeof(double)) != cudaSuccess ||
+        cudaMemcpy(P->lam_i, li.data(), m * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(P->lam_j, lj.data(), m * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
         dst_plan_destroy(P);
         return CNV_CUDA_ERROR;
     }
-    if (cudaMemcpy(P->S, S.data(), mm * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(P->li, li.data(), m * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(P->lj, lj.data(), m * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
-        dst_plan_destroy(P);
-        return CNV_CUDA_ERROR;
-    }
-    // more, smaller blocks when the grid is small, so that every SM gets work
-    int sms = 148;
-    int dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    P->rows = (ceil_div(m, kCols) * ceil_div((m + 1) / 2, 16) >= 2 * sms) ? 16 : (ceil_div(m, kCols) * ceil_div((m + 1) / 2, 8) >= 2 * sms) ? 8 : 4;
     return CNV_OK;
 }
 
@@ -239,18 +414,20 @@ void dst_plan_destroy(DstPlan* P) {
     cudaFree(P->S);
     cudaFree(P->t1);
     cudaFree(P->t2);
-    cudaFree(P->li);
-    cudaFree(P->lj);
+    cudaFree(P->lam_i);
+    cudaFree(P->lam_j);
+    cudaFree(P->tw);
+    cudaFree(P->cs);
     *P = DstPlan{};
 }
 
 cudaError_t dst_solve(const DstPlan& P, const double* in, double scale, double* out, cudaStream_t s) {
-    return solve_any(P, in, scale, DstDest{out, P.n, 1, nullptr, nullptr, 0}, s);
+    return solve(P, in, scale, DstDest{out, P.n, 1, nullptr, nullptr, 0, 0, nullptr, nullptr}, s);
 }
 
 cudaError_t dst_solve_split(const DstPlan& P, const double* in, double scale, double* red, double* black, int pitch,
                             cudaStream_t s) {
-    return solve_any(P, in, scale, DstDest{nullptr, 0, 1, red, black, pitch}, s);
+    return solve(P, in, scale, DstDest{nullptr, 0, 1, red, black, pitch, 0, nullptr, nullptr}, s);
 }
 
 }  // namespace cnv

@@ -3,7 +3,12 @@
 It must give the answer the reference's SOR converges to: the oracle's red-black SOR run to a
 stop norm near rounding (sum|dpsi| < 1e-15 for one solve, < 1e-13 in time steps) is the check, to 1e-11 normwise
 relative for a solve and 1e-10 for whole time steps. It must also beat the FP64 SOR path's own
-error against that converged answer by orders of magnitude.
+error against that converged answer by orders of magnitude. On grids too large for the oracle's
+SOR it must match the sine-transform solve psi = S((S R S) ./ Lambda) S done densely in numpy FP64,
+with the eigenvalues as sums of squared sines (accurate to a few units of rounding against an
+extended-precision solve), to 1e-13, on both of its row-transform paths: the FFT (2(n-1) has only
+prime factors up to 251) and the dense products (n = 258: 2 * 257). The eigenvalues written as
+den - 2 dy^2 cos - 2 dx^2 cos instead lose accuracy as n grows (about 2e-12 at n = 1024).
 """
 from __future__ import annotations
 
@@ -12,6 +17,7 @@ import pytest
 
 SOLVE_TOL = 1e-11   # direct solve vs converged oracle SOR, normwise relative
 STEP_TOL = 1e-10    # fields after several steps
+DENSE_TOL = 1e-13   # direct solve vs the dense sine-transform solve in numpy
 
 
 def _rel(a, b):
@@ -32,6 +38,37 @@ def test_direct_solve_matches_converged_sor(cnv, orc, n):
     assert rc == 0 and iters == 0 and e == 0.0
     assert np.all(got[0] == 0) and np.all(got[-1] == 0) and np.all(got[:, 0] == 0) and np.all(got[:, -1] == 0)
     assert _rel(got, want) <= SOLVE_TOL
+
+
+def _dense_sine_solve(f, dx, dy):
+    """psi for the reference's right-hand side f (the equation den psi - dy^2 (psi_i+1 + psi_i-1)
+    - dx^2 (psi_j+1 + psi_j-1) = -c4 f on the interior, psi = 0 on the edge) by four dense
+    products with the orthonormal DST-I matrix, in numpy FP64; the eigenvalues
+    4 dy^2 sin^2(pi a / 2(m+1)) + 4 dx^2 sin^2(pi b / 2(m+1))."""
+    n = f.shape[0]
+    m = n - 2
+    k = np.arange(1, m + 1)
+    arg = np.outer(k, k) % (2 * (m + 1))  # exact argument reduction
+    S = np.sqrt(2.0 / (m + 1)) * np.sin(np.pi * arg / (m + 1))
+    sk = np.sin(np.pi * k / (2 * (m + 1)))
+    lam = 4 * dy * dy * (sk * sk)[:, None] + 4 * dx * dx * (sk * sk)[None, :]
+    R = -(dx * dx * dy * dy) * f[1:-1, 1:-1]
+    out = np.zeros_like(f)
+    out[1:-1, 1:-1] = S @ ((S @ R @ S) / lam) @ S
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,L", [(37, 1), (96, 2), (258, 1), (1024, 1)])
+def test_direct_solve_matches_dense_sine_transform_solve(cnv, n, L):
+    rng = np.random.default_rng(n + 7)
+    f = rng.standard_normal((n, n))
+    cfg = cnv.default_config(nx=n, ny=n, Lx=L, Ly=1, poisson_type=cnv.POISSON_DIRECT)
+    with cnv.Cavity(cfg) as cav:
+        rc, got, _, _ = cav.poisson(f)
+    assert rc == 0
+    want = _dense_sine_solve(f, L / n, 1.0 / n)
+    assert _rel(got, want) <= DENSE_TOL
 
 
 @pytest.mark.gpu
