@@ -89,16 +89,14 @@ struct SyncState {
     // that every contribution is a fire-and-forget add with no carry between words
     unsigned long long acc[kRing][4];
     unsigned int count[kRing];
-    unsigned int fp64[kRing];   // a block added an FP64 part (cells with |psi| >= 2^46) to fsum
-    double fsum[kRing];
+    double fsum[kRing];         // FP64 part of e_k (cells with |psi| >= 2^46), usually 0
     unsigned int flag[2][kMaxSolverBlocks];  // [colour][block]: last sweep whose frame is written
 };
 
 // Block-shared state of the two warp roles.
 struct Shared {
     unsigned long long part[2][kCellWarps][4];  // [sweep parity][warp] norm chunk sums
-    unsigned int pfp[2][kCellWarps];             // the warp's FP64 part of the norm is pfs
-    double pfs[2][kCellWarps];
+    double side[2];                             // [sweep parity] FP64 side sum of the norm
     unsigned int ctr[2];                        // interior chunk counters, by half-sweep parity
     int stop[2];                                // verdict before sweep k, at [k & 1]
     int status, conv_k;
@@ -155,7 +153,7 @@ struct SweepPtrs {
 template <Arith A, int KIND, bool FOLD, bool FRAME>
 __device__ __forceinline__ void update_cell(const PoissonParams& p, int i, int j, const double* __restrict__ S_prev,
                                             double* __restrict__ S_new, const double* __restrict__ O,
-                                            const double* __restrict__ rhs, NormAcc& acc) {
+                                            const double* __restrict__ rhs, NormAcc& acc, double* side) {
     const size_t row = (size_t)i * p.pitch;
     const int m = j >> 1;
     const double old = ld<FRAME>(S_prev + row + m);
@@ -163,7 +161,7 @@ __device__ __forceinline__ void update_cell(const PoissonParams& p, int i, int j
     const double dn = ld<FRAME>(O + row - p.pitch + m);
     const double lt = ld<FRAME>(O + row + ((j - 1) >> 1));
     const double rt = ld<FRAME>(O + row + ((j + 1) >> 1));
-    S_new[row + m] = point_update<A, KIND, FOLD>(p, up, dn, rt, lt, __ldg(rhs + row + m), old, acc);
+    S_new[row + m] = point_update<A, KIND, FOLD>(p, up, dn, rt, lt, __ldg(rhs + row + m), old, acc, side);
 }
 
 // x / d for 0 <= x < 2^31 and 1 <= d, with m = 0xffffffff / d: the multiply-high estimate is
@@ -181,7 +179,7 @@ __device__ __forceinline__ int div_magic(int x, int d, unsigned m) {
 // region's first cell and store nothing.
 template <Arith A, int KIND, bool FOLD, int C>
 __device__ __forceinline__ void interior_chunks(const PoissonParams& p, const Tile& t, const SweepPtrs& q,
-                                                NormAcc& acc, unsigned* ctr) {
+                                                NormAcc& acc, unsigned* ctr, double* side) {
     const int w = t.ci1 - t.ci0;
     const int h = t.ri1 - t.ri0;
     if (w <= 0 || h <= 0) return;
@@ -206,9 +204,11 @@ __device__ __forceinline__ void interior_chunks(const PoissonParams& p, const Ti
                 const int j = t.ci0 + 2 * (xx - r * wq) + ((i + t.ci0 + cc) & 1);
                 if (j < t.ci1) {
                     if (cc)
-                        update_cell<A, KIND, FOLD, false>(p, i, j, q.prev[1], q.next[1], q.oth[1], q.rhs[1], acc);
+                        update_cell<A, KIND, FOLD, false>(p, i, j, q.prev[1], q.next[1], q.oth[1], q.rhs[1], acc,
+                                                          side);
                     else
-                        update_cell<A, KIND, FOLD, false>(p, i, j, q.prev[0], q.next[0], q.oth[0], q.rhs[0], acc);
+                        update_cell<A, KIND, FOLD, false>(p, i, j, q.prev[0], q.next[0], q.oth[0], q.rhs[0], acc,
+                                                          side);
                 }
             }
         }
@@ -257,7 +257,7 @@ __device__ __forceinline__ void interior_chunks(const PoissonParams& p, const Ti
             const double nw = point_value<A, KIND, FOLD>(p, up[u], dn[u], rt[u], lt[u], g[u], old[u]);
             if (ok[u]) {
                 Sn[at[u]] = nw;
-                norm_add(acc, nw, old[u]);
+                if (!norm_add(acc, nw, old[u])) norm_side_add(side, nw, old[u]);
             }
         }
     }
@@ -267,7 +267,7 @@ __device__ __forceinline__ void interior_chunks(const PoissonParams& p, const Ti
 // out over the kFrameThreads threads of the frame warps.
 template <Arith A, int KIND, bool FOLD, int C>
 __device__ __forceinline__ void frame_pass(const PoissonParams& p, const Tile& t, const SweepPtrs& q,
-                                           NormAcc& acc) {
+                                           NormAcc& acc, double* side) {
     const int W = t.c1 - t.c0;
     const int top = t.ri0 - t.r0, bot = t.r1 - t.ri1;
     const int left = t.ci0 - t.c0, right = t.c1 - t.ci1;
@@ -291,34 +291,28 @@ __device__ __forceinline__ void frame_pass(const PoissonParams& p, const Tile& t
         const int cc = (i + j) & 1;
         if (C != 2) {
             if (cc != C) continue;
-            update_cell<A, KIND, FOLD, true>(p, i, j, q.prev[C], q.next[C], q.oth[C], q.rhs[C], acc);
+            update_cell<A, KIND, FOLD, true>(p, i, j, q.prev[C], q.next[C], q.oth[C], q.rhs[C], acc, side);
         } else if (cc) {
-            update_cell<A, KIND, FOLD, true>(p, i, j, q.prev[1], q.next[1], q.oth[1], q.rhs[1], acc);
+            update_cell<A, KIND, FOLD, true>(p, i, j, q.prev[1], q.next[1], q.oth[1], q.rhs[1], acc, side);
         } else {
-            update_cell<A, KIND, FOLD, true>(p, i, j, q.prev[0], q.next[0], q.oth[0], q.rhs[0], acc);
+            update_cell<A, KIND, FOLD, true>(p, i, j, q.prev[0], q.next[0], q.oth[0], q.rhs[0], acc, side);
         }
     }
 }
 
 // Signal warp, lane 0: adds this block's share of e_k (the cell warps' chunk sums of sweep k,
-// in sh.part[k & 1]) to ring slot k % kRing and counts the block in.
-__device__ __forceinline__ void contribute(SyncState* sy, int k, const Shared& sh) {
+// in sh.part[k & 1], and the FP64 side sum sh.side[k & 1], which it clears for sweep k + 2) to
+// ring slot k % kRing and counts the block in.
+__device__ __forceinline__ void contribute(SyncState* sy, int k, Shared& sh) {
     unsigned long long s[4] = {0, 0, 0, 0};
-    unsigned fp = 0;
-    double fs = 0.0;
     for (int w = 0; w < kCellWarps; ++w) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) s[c] += sh.part[k & 1][w][c];
-        if (sh.pfp[k & 1][w]) {
-            fp = 1;
-            fs = __dadd_rn(fs, sh.pfs[k & 1][w]);
-        }
     }
     const int slot = k % kRing;
-    if (fp) {
-        atomicAdd(&sy->fsum[slot], fs);
-        atomicOr(&sy->fp64[slot], 1u);
-    }
+    const double fs = sh.side[k & 1];
+    sh.side[k & 1] = 0.0;
+    if (fs != 0.0 || fs != fs) atomicAdd(&sy->fsum[slot], fs);  // only where a cell reached 2^46
 #pragma unroll
     for (int c = 0; c < 4; ++c) atomicAdd(&sy->acc[slot][c], s[c]);
     __threadfence();
@@ -333,8 +327,7 @@ __device__ int check_norm(SyncState* sy, int j, const PoissonParams& p, Ctrl* ct
     unsigned long long c[4];
 #pragma unroll
     for (int w = 0; w < 4; ++w) c[w] = __ldcg(&sy->acc[slot][w]);
-    *e = norm_total(c);
-    if (__ldcg(&sy->fp64[slot])) *e = __dadd_rn(*e, __ldcg(&sy->fsum[slot]));
+    *e = __dadd_rn(norm_total(c), __ldcg(&sy->fsum[slot]));
     if (!isfinite(*e)) return 3;
     return *e < p.tol ? 1 : 0;
 }
@@ -367,7 +360,6 @@ __device__ void signal_warp(const PoissonParams& p, const Tile& t, SyncState* sy
                 const int slot = (k - 4) % kRing;
 #pragma unroll
                 for (int w = 0; w < 4; ++w) sy->acc[slot][w] = 0;
-                sy->fp64[slot] = 0;
                 sy->fsum[slot] = 0.0;
                 __threadfence();
                 atomicExch(&sy->count[slot], 0u);
@@ -463,17 +455,18 @@ __device__ void cell_warps(const PoissonLaunch& L, const Tile& t, Shared& sh) {
         q.next[1] = odd ? s1b : s0b;
         q.rhs[0] = L.rhs[0];
         q.rhs[1] = L.rhs[1];
-        NormAcc acc{{0, 0, 0, 0}, 0, 0.0};
+        NormAcc acc{{0, 0, 0, 0}};
+        double* const side = &sh.side[k & 1];
         if (KIND == CNV_POISSON_JACOBI) {
             q.oth[0] = q.prev[1];
             q.oth[1] = q.prev[0];
             if (frame_warp) {
                 bar_sync(kBarGo, kGoThreads);
-                frame_pass<A, KIND, FOLD, 2>(p, t, q, acc);
+                frame_pass<A, KIND, FOLD, 2>(p, t, q, acc, side);
                 __syncwarp();
                 bar_arrive(kBarPub, kGoThreads);
             }
-            interior_chunks<A, KIND, FOLD, 2>(p, t, q, acc, &sh.ctr[half & 1]);
+            interior_chunks<A, KIND, FOLD, 2>(p, t, q, acc, &sh.ctr[half & 1], side);
             bar_sync(kBarEnd, kCellThreads);
             if (threadIdx.x == 0) sh.ctr[half & 1] = 0;
             ++half;
@@ -483,21 +476,21 @@ __device__ void cell_warps(const PoissonLaunch& L, const Tile& t, Shared& sh) {
             q.oth[1] = q.next[0];  // black: red of sweep k (new), own black of sweep k-1
             if (frame_warp) {
                 bar_sync(kBarGo, kGoThreads);
-                frame_pass<A, KIND, FOLD, 0>(p, t, q, acc);
+                frame_pass<A, KIND, FOLD, 0>(p, t, q, acc, side);
                 __syncwarp();
                 bar_arrive(kBarPub, kGoThreads);
             }
-            interior_chunks<A, KIND, FOLD, 0>(p, t, q, acc, &sh.ctr[half & 1]);
+            interior_chunks<A, KIND, FOLD, 0>(p, t, q, acc, &sh.ctr[half & 1], side);
             bar_sync(kBarEnd, kCellThreads);
             if (threadIdx.x == 0) sh.ctr[half & 1] = 0;
             ++half;
             if (frame_warp) {
                 bar_sync(kBarGo, kGoThreads);
-                frame_pass<A, KIND, FOLD, 1>(p, t, q, acc);
+                frame_pass<A, KIND, FOLD, 1>(p, t, q, acc, side);
                 __syncwarp();
                 bar_arrive(kBarPub, kGoThreads);
             }
-            interior_chunks<A, KIND, FOLD, 1>(p, t, q, acc, &sh.ctr[half & 1]);
+            interior_chunks<A, KIND, FOLD, 1>(p, t, q, acc, &sh.ctr[half & 1], side);
             bar_sync(kBarEnd, kCellThreads);
             if (threadIdx.x == 0) sh.ctr[half & 1] = 0;
             ++half;
@@ -511,18 +504,9 @@ __device__ void cell_warps(const PoissonLaunch& L, const Tile& t, Shared& sh) {
             for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
             acc.c[w] = x;
         }
-        const unsigned fp = __any_sync(0xffffffffu, acc.fp64) ? 1u : 0u;
-        double fs = 0.0;
-        if (fp) {  // only where a cell reached 2^46: the FP64 part, summed over the warp
-            fs = acc.fsum;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) fs = __dadd_rn(fs, __shfl_xor_sync(0xffffffffu, fs, off));
-        }
         if ((threadIdx.x & 31) == 0) {
 #pragma unroll
             for (int w = 0; w < 4; ++w) sh.part[k & 1][warp][w] = acc.c[w];
-            sh.pfp[k & 1][warp] = fp;
-            sh.pfs[k & 1][warp] = fs;
         }
         __syncwarp();
         bar_arrive(kBarNorm, kThreads);
@@ -541,6 +525,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_poisson(PoissonLaunch L) {
     if (threadIdx.x < 2) {
         sh.ctr[threadIdx.x] = 0;
         sh.stop[threadIdx.x] = 0;
+        sh.side[threadIdx.x] = 0.0;
     }
     if (threadIdx.x == 0) s_abort = ld_volatile_int(&ctl->abort);
     __syncthreads();

@@ -43,8 +43,7 @@ constexpr int kTbSnap = 4;               // snapshots of psi kept in global memo
 
 struct TbSync {
     unsigned long long acc[kTbRing][kTbMaxSweeps][4];  // e_k * 2^80 as 32-bit chunks in 64-bit counters
-    unsigned int fp64[kTbRing][kTbMaxSweeps];        // fsum holds a part (cells with |psi| >= 2^46)
-    double fsum[kTbRing][kTbMaxSweeps];
+    double fsum[kTbRing][kTbMaxSweeps];             // FP64 part of e_k (cells with |psi| >= 2^46), usually 0
     unsigned int count[kTbRing];                    // blocks that added their share of an epoch
     unsigned int flag[kMaxSolverBlocks];            // epochs a block has completed (snapshot written)
 };
@@ -94,8 +93,7 @@ __device__ __forceinline__ TbGeom tb_geom(const TbTile& t) {
 // shared-memory tile. psi of colour c at sc, of the other colour at so; the right-hand side of
 // colour c at gs (shared, same geometry) or gg (global split layout, pitch P). With NORM, cells
 // of the owned box add |new - old| to this thread's accumulator, which is reduced per warp and
-// added to s_sum (4 chunks) at the end, with any FP64 part (cells with |psi| >= 2^46) in s_fsum
-// and flagged in s_fp.
+// added to s_sum (4 chunks) at the end; owned cells with |psi| >= 2^46 add to s_fsum in FP64.
 extern __shared__ double tb_smem[];
 
 template <Arith A, int KIND, bool FOLD, bool G_SMEM, bool NORM>
@@ -103,13 +101,13 @@ __device__ __forceinline__ void tb_half_sweep(const PoissonParams& p, int sc_off
                                               const double* __restrict__ gglob, int g_off, TbGeom G, int lo_r,
                                               int hi_r, int lo_c, int hi_c, int c, int own_r0, int own_r1,
                                               int own_c0, int own_c1, unsigned long long* s_sum,
-                                              unsigned int* s_fp, double* s_fsum) {
+                                              double* s_fsum) {
     // split columns of a row of parity q = (i + c) & 1 (cell j = 2m + q)
     const int mlo0 = fhalf(lo_c + 1), mhi0 = fhalf(hi_c - 1);       // q = 0
     const int mlo1 = fhalf(lo_c), mhi1 = fhalf(hi_c - 2);           // q = 1
     const int w = max(mhi0 - mlo0, mhi1 - mlo1) + 1;
     const int rows = hi_r - lo_r;
-    NormAcc acc{{0, 0, 0, 0}, 0, 0.0};
+    NormAcc acc{{0, 0, 0, 0}};
     if (w > 0 && rows > 0) {
         const int total = rows * w;
         const int swm = G.swm;
@@ -129,17 +127,12 @@ __device__ __forceinline__ void tb_half_sweep(const PoissonParams& p, int sc_off
             const double rt = tb_smem[so_off + k + q];
             const double g = G_SMEM ? tb_smem[g_off + k] : __ldg(gglob + (size_t)i * p.pitch + m);
             // one update for every cell (no divergence on the FP64 path); only owned cells count
-            NormAcc one{{0, 0, 0, 0}, 0, 0.0};
-            tb_smem[sc_off + k] = point_update<A, KIND, FOLD>(p, up, dn, rt, lt, g, old, one);
+            const double nw = point_value<A, KIND, FOLD>(p, up, dn, rt, lt, g, old);
+            tb_smem[sc_off + k] = nw;
             if (NORM) {
                 const int j = 2 * m + q;
                 if (i >= own_r0 && i < own_r1 && j >= own_c0 && j < own_c1) {
-#pragma unroll
-                    for (int kk = 0; kk < 4; ++kk) acc.c[kk] += one.c[kk];
-                    if (one.fp64) {
-                        acc.fp64 = 1;
-                        acc.fsum = __dadd_rn(acc.fsum, one.fsum);
-                    }
+                    if (!norm_add(acc, nw, old)) norm_side_add(s_fsum, nw, old);
                 }
             }
         }
@@ -152,21 +145,10 @@ __device__ __forceinline__ void tb_half_sweep(const PoissonParams& p, int sc_off
             for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
             acc.c[k] = v;
         }
-        const bool fp = __any_sync(0xffffffffu, acc.fp64);
-        double fs = 0.0;
-        if (fp) {
-            fs = acc.fsum;
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) fs = __dadd_rn(fs, __shfl_xor_sync(0xffffffffu, fs, off));
-        }
         if ((threadIdx.x & 31) == 0) {
 #pragma unroll
             for (int k = 0; k < 4; ++k)
                 if (acc.c[k]) atomicAdd(s_sum + k, acc.c[k]);
-            if (fp) {
-                atomicAdd(s_fsum, fs);
-                atomicOr(s_fp, 1u);
-            }
         }
     }
 }
@@ -226,7 +208,7 @@ __device__ void tb_store_own(const TbTile& t, const TbGeom& G, double* const* sp
 template <int S, Arith A, int KIND, bool FOLD, bool G_SMEM>
 __device__ __forceinline__ void tb_sweeps(const TbLaunchDev& L, const TbTile& t, const TbGeom& G, int plane,
                                           int nsweeps, bool norm, unsigned long long (*s_sum)[4],
-                                          unsigned int* s_fp, double* s_fsum) {
+                                          double* s_fsum) {
     const int n = L.p.n;
     for (int sw = 0; sw < nsweeps; ++sw) {
         for (int c = 0; c < 2; ++c) {
@@ -238,10 +220,10 @@ __device__ __forceinline__ void tb_sweeps(const TbLaunchDev& L, const TbTile& t,
             const double* gg = c ? L.rhs[1] : L.rhs[0];
             if (norm)
                 tb_half_sweep<A, KIND, FOLD, G_SMEM, true>(L.p, sc, so, gg, go, G, lo_r, hi_r, lo_c, hi_c, c, t.r0,
-                                                           t.r1, t.c0, t.c1, s_sum[sw], s_fp + sw, s_fsum + sw);
+                                                           t.r1, t.c0, t.c1, s_sum[sw], s_fsum + sw);
             else
                 tb_half_sweep<A, KIND, FOLD, G_SMEM, false>(L.p, sc, so, gg, go, G, lo_r, hi_r, lo_c, hi_c, c,
-                                                            t.r0, t.r1, t.c0, t.c1, nullptr, nullptr, nullptr);
+                                                            t.r0, t.r1, t.c0, t.c1, nullptr, nullptr);
             __syncthreads();
         }
     }
@@ -253,7 +235,6 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_poisson_tb(TbLaunchDev L) {
     if (ctl->abort) return;
     double* const s_dyn = tb_smem;
     __shared__ unsigned long long s_sum[kTbMaxSweeps][4];
-    __shared__ unsigned int s_fp[kTbMaxSweeps];
     __shared__ double s_fsum[kTbMaxSweeps];
     __shared__ int s_ok[8];
     __shared__ int s_res, s_k;
@@ -300,8 +281,7 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_poisson_tb(TbLaunchDev L) {
                     unsigned long long c[4];
 #pragma unroll
                     for (int w = 0; w < 4; ++w) c[w] = __ldcg(&sy->acc[slot][s][w]);
-                    double e = norm_total(c);
-                    if (__ldcg(&sy->fp64[slot][s])) e = __dadd_rn(e, __ldcg(&sy->fsum[slot][s]));
+                    const double e = __dadd_rn(norm_total(c), __ldcg(&sy->fsum[slot][s]));
                     s_e = e;
                     s_k = X * S + s + 1;
                     if (!isfinite(e)) res = 3;
@@ -330,7 +310,6 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_poisson_tb(TbLaunchDev L) {
                 for (int s = 0; s < kTbMaxSweeps; ++s) {
 #pragma unroll
                     for (int w = 0; w < 4; ++w) sy->acc[slot][s][w] = 0;
-                    sy->fp64[slot][s] = 0;
                     sy->fsum[slot][s] = 0.0;
                 }
                 __threadfence();
@@ -350,23 +329,18 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_poisson_tb(TbLaunchDev L) {
             tb_load(L, t, G, sp, (E - 1) % kTbSnap, true);
         }
         if (threadIdx.x < kTbMaxSweeps * 4) s_sum[threadIdx.x / 4][threadIdx.x % 4] = 0;
-        if (threadIdx.x < kTbMaxSweeps) {
-            s_fp[threadIdx.x] = 0;
-            s_fsum[threadIdx.x] = 0.0;
-        }
+        if (threadIdx.x < kTbMaxSweeps) s_fsum[threadIdx.x] = 0.0;
         __syncthreads();
         const int ns = min(S, kmax - E * S);
-        tb_sweeps<S, A, KIND, FOLD, G_SMEM>(L, t, G, plane, ns, true, s_sum, s_fp, s_fsum);
+        tb_sweeps<S, A, KIND, FOLD, G_SMEM>(L, t, G, plane, ns, true, s_sum, s_fsum);
         // this block's shares of e for the epoch's sweeps, then the epoch count
         const int slot = E % kTbRing;
         if (threadIdx.x < ns * 4) {
             const unsigned long long v = s_sum[threadIdx.x / 4][threadIdx.x % 4];
             if (v) atomicAdd(&sy->acc[slot][threadIdx.x / 4][threadIdx.x % 4], v);
         } else if (threadIdx.x >= 32 && threadIdx.x < 32 + ns) {
-            if (s_fp[threadIdx.x - 32]) {
-                atomicAdd(&sy->fsum[slot][threadIdx.x - 32], s_fsum[threadIdx.x - 32]);
-                atomicOr(&sy->fp64[slot][threadIdx.x - 32], 1u);
-            }
+            const double fs = s_fsum[threadIdx.x - 32];
+            if (fs != 0.0 || fs != fs) atomicAdd(&sy->fsum[slot][threadIdx.x - 32], fs);
         }
         // own cells -> snapshot slot E % kTbSnap
         tb_store_own(t, G, sp, snap_at(L, E % kTbSnap, 0), snap_at(L, E % kTbSnap, 1), P);
@@ -394,7 +368,7 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_poisson_tb(TbLaunchDev L) {
         __syncthreads();
         tb_load(L, t, G, sp, X > 0 ? (X - 1) % kTbSnap : -1, false);
         __syncthreads();
-        tb_sweeps<S, A, KIND, FOLD, G_SMEM>(L, t, G, plane, conv_k - X * S, false, nullptr, nullptr, nullptr);
+        tb_sweeps<S, A, KIND, FOLD, G_SMEM>(L, t, G, plane, conv_k - X * S, false, nullptr, nullptr);
     }
     tb_store_own(t, G, sp, L.out[0], L.out[1], P);
     if (me == 0 && threadIdx.x == 0) {

@@ -87,13 +87,18 @@ __host__ __device__ __forceinline__ double norm_total(const unsigned long long c
 // multiple of 2^-80 first: values of 2^-28 or more are multiples already, so a cell is off by
 // less than 2^-80 only when one of its values lies below 2^-28, and the total is off by less than
 // (number of cells) * 2^-80 (about 1e-18 at 1024^2). Cells with a value of 2^46 or more (or a
-// non-finite one) are summed in FP64 instead (fsum, flagged by fp64): they are far outside any
-// realistic streamfunction, and the reference sums them in FP64 too.
+// non-finite one) are left to the caller, which adds them to an FP64 side sum in shared memory
+// (norm_side_add): they are far outside any realistic streamfunction, and the reference sums them
+// in FP64 too. The side sum lives outside the accumulator so that the sweep loops carry only the
+// four integer chunks.
 struct NormAcc {
     unsigned long long c[4];
-    unsigned int fp64;  // set once fsum holds a cell
-    double fsum;
 };
+
+// |nw - old| into an FP64 side sum (a block's shared accumulator): the rare cells norm_add leaves.
+__device__ __noinline__ void norm_side_add(double* side, double nw, double old) {
+    atomicAdd(side, fabs(__dsub_rn(nw, old)));
+}
 
 // |x| * 2^80, truncated, as a 128-bit integer (hi:lo), for |x| < 2^46; values below 2^-80 give 0.
 __device__ __forceinline__ void abs_fixed80(double x, unsigned long long& lo, unsigned long long& hi) {
@@ -114,9 +119,9 @@ __device__ __forceinline__ void abs_fixed80(double x, unsigned long long& lo, un
     }
 }
 
-// acc += |nw - old|: exactly in fixed point (both truncated at 2^-80) on the integer pipes, or in
-// FP64 when a value reaches 2^46.
-__device__ __forceinline__ void norm_add(NormAcc& acc, double nw, double old) {
+// acc += |nw - old| exactly in fixed point (both truncated at 2^-80) on the integer pipes. Returns
+// false, adding nothing, when a value reaches 2^46 or is not finite (the caller's FP64 side sum).
+__device__ __forceinline__ bool norm_add(NormAcc& acc, double nw, double old) {
     {
         // the common case, same sign and exponent e with 2^-28 <= |x| < 2^46: both images are
         // exact (no truncation), and their difference is the significands' difference (the
@@ -143,16 +148,12 @@ __device__ __forceinline__ void norm_add(NormAcc& acc, double nw, double old) {
             acc.c[1] += dl >> 32;
             acc.c[2] += dh & 0xffffffffull;
             acc.c[3] += dh >> 32;
-            return;
+            return true;
         }
     }
     if (((unsigned long long)__double_as_longlong(nw) & 0x7fffffffffffffffull) >= (1069ull << 52) ||
-        ((unsigned long long)__double_as_longlong(old) & 0x7fffffffffffffffull) >= (1069ull << 52)) {
-        // a value of 2^46 or more, Inf or NaN: the FP64 part of the norm
-        acc.fsum = __dadd_rn(acc.fsum, fabs(__dsub_rn(nw, old)));
-        acc.fp64 = 1;
-        return;
-    }
+        ((unsigned long long)__double_as_longlong(old) & 0x7fffffffffffffffull) >= (1069ull << 52))
+        return false;  // a value of 2^46 or more, Inf or NaN: the FP64 side sum
     unsigned long long al, ah, bl, bh;
     abs_fixed80(nw, al, ah);
     abs_fixed80(old, bl, bh);
@@ -174,6 +175,7 @@ __device__ __forceinline__ void norm_add(NormAcc& acc, double nw, double old) {
     acc.c[1] += dl >> 32;
     acc.c[2] += dh & 0xffffffffull;
     acc.c[3] += dh >> 32;
+    return true;
 }
 
 __device__ __forceinline__ bool big_or_zero(double x) {
@@ -283,12 +285,13 @@ __device__ __forceinline__ double point_value(const PoissonParams& p, double up,
     }
 }
 
-// The new value of one cell, with |new - old| added to the stop norm.
+// The new value of one cell, with |new - old| added to the stop norm (to the FP64 side sum *side
+// for a value of 2^46 or more).
 template <Arith A, int KIND, bool FOLD>
 __device__ __forceinline__ double point_update(const PoissonParams& p, double up, double dn, double rt,
-                                               double lt, double g, double old, NormAcc& acc) {
+                                               double lt, double g, double old, NormAcc& acc, double* side) {
     const double nw = point_value<A, KIND, FOLD>(p, up, dn, rt, lt, g, old);
-    norm_add(acc, nw, old);
+    if (!norm_add(acc, nw, old)) norm_side_add(side, nw, old);
     return nw;
 }
 

@@ -210,6 +210,31 @@ def test_1024_four_steps_match_oracle(cnv, orc):
         assert bitwise(a, b), name
 
 
+def test_1024_fifty_steps_match_oracle(cnv, orc):
+    """The benchmark workload for 50 steps (about 125,000 SOR sweeps, into the range the
+    benchmark times): every step's iteration count, continuity max and min, and the final fields
+    bit for bit, against the oracle on all host cores (its parallel row-sum stop norm; the GPU's
+    is order-free, and the two could differ only at a tie of the norm with tol within rounding)."""
+    n, steps = 1024, 50
+    h = 1.0 / n
+    dt = 0.2 * min(h * h * 1000.0 / 4, h / 1.0)
+    cfg = make_cfg(cnv, n, Re=1000.0, dt=dt, poisson_tol=1e-6, poisson_max_it=100000)
+    with cnv.Cavity(cfg) as cav:
+        rc, gsteps = cav.step(steps)
+        g = cav.get_fields()
+    assert rc == 0
+    p = orc.make_params(n, order=cfg.order, re=cfg.Re, dt=cfg.dt, tol=cfg.poisson_tol, itmax=cfg.poisson_max_it,
+                        threads=os.cpu_count() or 1, exact_norm=0)
+    w, u, v, psi = orc.initial_state(n)
+    orc_rc, osteps = orc.run(p, steps, w, u, v, psi)
+    assert orc_rc == 0
+    assert [s["iters"] for s in gsteps] == [s["iters"] for s in osteps]
+    for a, b in zip(gsteps, osteps):
+        assert a["cont_max"] == b["cont_max"] and a["cont_min"] == b["cont_min"]
+    for name, a, b in zip("w u v psi".split(), g, (w, u, v, psi)):
+        assert bitwise(a, b), name
+
+
 @pytest.mark.parametrize("blocking", [1, 4])
 @pytest.mark.parametrize("ptype", [1, 2])
 def test_poisson_with_streamfunction_beyond_2_46(cnv, orc, ptype, blocking):
