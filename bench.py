@@ -209,6 +209,30 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+# The two passes around the Poisson solve, per cell: algorithmic bytes (each field read or written
+# once; halo re-reads not counted) and FP64 add/multiply operations on interior cells.
+PRE_BYTES, PRE_OPS = 40, 66    # read w, u, v; write w_out and the right-hand side; 4 x 14 + 8 + 2
+POST_BYTES, POST_OPS = 32, 57  # read psi; write u, v, psi; 2 x 14 (velocity) + 2 x 14 + 1 (continuity)
+
+
+def step_passes(cnvpy, local, n, add_mul_rate, peak_gbs, reps=50):
+    """k_pre and k_post timed alone (cnv_time_passes) on an n^2 cavity after one step, against the
+    HBM peak and the device's FP64 add/multiply rate."""
+    w = workload(n)
+    with cnvpy.Cavity(make_config(cnvpy, w, local)) as cav:
+        cav.step(1)
+        pre_ms, post_ms = cav.time_passes(reps)
+    cells = n * n
+    out = {}
+    for name, ms, nb, ops in (("k_pre", pre_ms, PRE_BYTES, PRE_OPS), ("k_post", post_ms, POST_BYTES, POST_OPS)):
+        gbs = cells * nb / (ms * 1e-3) / 1e9
+        gops = cells * ops / (ms * 1e-3) / 1e9
+        out[name] = {"ms": round(ms, 4), "bytes_per_cell": nb, "achieved_gbs": round(gbs, 1),
+                     "hbm_frac": round(gbs / peak_gbs, 4), "fp64_ops_per_cell": ops, "fp64_gops": round(gops, 1),
+                     "fp64_frac": round(gops * 1e9 / add_mul_rate, 4) if add_mul_rate else None}
+    return out
+
+
 def form_adjoint(cnvpy, local, ndirs=16, n=256, steps=2000, every=100, eps=1e-6):
     """256^2 cavity, Re 400, 2000 steps, initial vorticity = seeded smooth Gaussian field: gradient
     of J = 1/2 sum w(T)^2 h^2 with respect to w0 and the lid speed by the adjoint kernels
@@ -369,18 +393,24 @@ def form_batched(cnvpy, local, steps, count=256, seed=0):
                                             enumerate(sorted({s["n"] for s in specs}))},
                       "cost_model_ms_per_step": round(cnvpy.batch_plan(specs)[1] / 1e3, 3),
                       "max_relative_residual": max(x["err"] for x in last)}
-    f_cells, f_ms, errs = 0, 0.0, {}
+    f_cells, f_ms, m_ms, errs = 0, 0.0, 0.0, {}
     for k in sample:
         sp = specs[k]
         h = 1.0 / sp["n"]
         dt = sp["dt"] or 0.2 * min(h * h * sp["Re"] / 4.0, h / abs(sp["lid"]))  # the batch's stable dt
         cfg = cnvpy.default_config(nx=sp["n"], ny=sp["n"], Re=sp["Re"], u4=sp["lid"], dt=dt,
-                                   poisson_tol=1e-6, poisson_max_it=1000000, device=local)
+                                   poisson_tol=1e-6, poisson_max_it=1000000, mixed_rtol=1e-10, device=local)
         with cnvpy.Cavity(cfg) as cav:
             cav.step(1)
             cav.step(steps)
             _, c_ms, _ = cav.stats()
             sor_fields = cav.get_fields()
+        cfg.precision = 2  # the mixed form alone: same solver as the batch, one cavity at a time
+        with cnvpy.Cavity(cfg) as cav:
+            cav.step(1)
+            cav.step(steps)
+            _, mc_ms, _ = cav.stats()
+        cfg.precision = 0
         cfg.poisson_type = 4
         with cnvpy.Cavity(cfg) as cav:
             cav.step(1 + steps)
@@ -389,12 +419,34 @@ def form_batched(cnvpy, local, steps, count=256, seed=0):
                                "fp64_sor_vs_converged_fp64": field_error(sor_fields, conv)}
         f_cells += sp["n"] ** 2
         f_ms += c_ms
-    out["fp64_cavity_by_cavity"] = {"value": mcells(f_cells, steps, f_ms), "unit": UNIT,
-                                    "sample": "one cavity of each size, each its own cnv_state, one call of "
-                                              f"{steps} steps"}
+        m_ms += mc_ms
+    sample_note = f"one cavity of each size, each its own cnv_state, one call of {steps} steps"
+    out["fp64_cavity_by_cavity"] = {"value": mcells(f_cells, steps, f_ms), "unit": UNIT, "sample": sample_note}
+    out["mixed_cavity_by_cavity"] = {"value": mcells(f_cells, steps, m_ms), "unit": UNIT, "sample": sample_note}
     out["errors"] = errs
     out["compared_after_steps"] = steps + 1
-    out["speedup_batched_over_fp64"] = round(out["batched"]["value"] / out["fp64_cavity_by_cavity"]["value"], 3)
+    b, f, m = out["batched"]["value"], out["fp64_cavity_by_cavity"]["value"], out["mixed_cavity_by_cavity"]["value"]
+    out["speedup_batched_over_fp64"] = round(b / f, 3)
+    out["speedup_mixed_over_fp64_cavity_by_cavity"] = round(m / f, 3)   # what the FP32 sweeps buy
+    out["speedup_batched_over_mixed_cavity_by_cavity"] = round(b / m, 3)  # what batching buys
+    out["cost_model_check"] = batch_model_check(cnvpy, local)
+    return out
+
+
+def batch_model_check(cnvpy, local, steps=20):
+    """The batch cost model's estimated step time against the measured one, on two small batches
+    where the model splits cavities that fit one block: ten 192^2 cavities, and five of 33^2..128^2."""
+    out = {}
+    for name, specs in (("ten_192", [dict(n=192, Re=1000.0, lid=1.0)] * 10),
+                        ("five_33_to_128", [dict(n=n, Re=1000.0, lid=1.0) for n in (33, 64, 96, 112, 128)])):
+        groups, est_us = cnvpy.batch_plan(specs)
+        with cnvpy.Batch(cnvpy.default_config(mixed_rtol=1e-10, device=local), specs) as bt:
+            bt.step(1)
+            bt.step(steps)
+            ms = bt.stats()[2] / steps
+            used = bt.groups()
+        out[name] = {"strips": used, "model_ms": round(est_us / 1e3, 3), "measured_ms": round(ms, 3),
+                     "model_error": round(est_us / 1e3 / ms - 1, 3), "planned_strips": groups}
     return out
 
 
@@ -488,11 +540,12 @@ def ours(args):
     peak, peak_kind = measured_peaks()
     traffic = POISSON_TRAFFIC["bytes_per_launch"] if args.form == "fp64" else None
     fp64 = None
+    add_mul = cnvpy.probe_fp64(local)[0]
     if args.form == "fp64":
         # the binding ceiling: the update's 7 FP64 add/multiply operations per interior cell-sweep
         # (5 on the FP64 pipe, the 2 multiplications by constants in exact integer arithmetic),
         # against the device's own FP64 rate for that mix (probe kernels, same process)
-        add_mul, fma_rate = cnvpy.probe_fp64(local)
+        fma_rate = cnvpy.probe_fp64(local)[1]
         ops = 7.0 * interior * sweeps / (pms * 1e-3)
         fp64 = {"achieved_gops": round(ops / 1e9, 1), "peak_gops": round(add_mul / 1e9, 1),
                 "frac": round(ops / add_mul, 4), "fma_peak_gops": round(fma_rate / 1e9, 1),
@@ -504,6 +557,8 @@ def ours(args):
     e2e = {"value": ws * cells * args.steps / e2e_s / 1e6, "unit": UNIT,
            "h2d_bytes_per_step": 3 * cells * 8, "d2h_bytes_per_step": 4 * cells * 8,
            "host_buffers": "pinned" if pinned else "pageable"}
+
+    passes = {str(n): step_passes(cnvpy, local, n, add_mul, peak) for n in (w["n"], 2 * w["n"])}
 
     forms = {}
     conv_err = None
@@ -543,7 +598,8 @@ def ours(args):
                      "traffic_source": POISSON_TRAFFIC["source"] if traffic else None, "peak_source": peak_kind,
                      "kernel": kernel, "fp64_pipe": fp64},
         "e2e": e2e,
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": 3 * args.steps,  # k_pre, k_poisson, k_post per step
+        "step_passes": passes,
         "clocks": clk,
         "forms": forms,
     }
@@ -594,6 +650,107 @@ def reference(args):
     print(json.dumps(line), flush=True)
 
 
+def full_config(args):
+    """One of the workloads run to its stated length (not part of the default run): a JSON line
+    with throughput sampled over windows of steps, sweeps per step, and the per-field error at the
+    end against the converged FP64 answer (the direct sine-transform solve of the same steps).
+        1: 64^2, Re 100, dt 1e-3, SOR factor 1.5, tol 1e-6, 1000 steps, against the CPU oracle
+        2: the 1024^2 headline workload, 10,000 steps: FP64 SOR, mixed and direct
+        3: 2048^2, Re 1000, smoothed-noise start, 5,000 steps: mixed and direct (FP64 SOR too
+           with --with-sor)
+        4: 256 uneven cavities, 2,000 steps: batched, against each size's direct run"""
+    import numpy as np
+
+    import cnvpy
+
+    cnvpy.load()
+    which = args.full_config
+    out = {"full_config": which, "unit": UNIT}
+
+    def windows(w, steps, window, **kw):
+        """Run steps in windows; per window: Mcell-steps/s from CUDA-event times and sweeps/step."""
+        cfg = make_config(cnvpy, w, 0, **kw)
+        rows, total_ms, sweeps_all = [], 0.0, 0
+        with cnvpy.Cavity(cfg) as cav:
+            done = 0
+            while done < steps:
+                k = min(window, steps - done)
+                rc, info = cav.step(k)
+                sw, ms, _ = cav.stats()
+                total_ms += ms
+                sweeps_all += sw
+                rows.append({"steps": [done, done + k - 1], "value": mcells(w["n"] ** 2, k, ms),
+                             "sweeps_per_step": round(sw / k, 1), "iters_last": info[-1]["iters"],
+                             "cont_max_last": info[-1]["cont_max"]})
+                done += k
+            fields = cav.get_fields()
+        return {"value": mcells(w["n"] ** 2, steps, total_ms), "steps": steps, "seconds": round(total_ms / 1e3, 2),
+                "sweeps_per_step": round(sweeps_all / steps, 1), "windows": rows}, fields
+
+    if which == 1:
+        import orc
+
+        n, steps = 64, 1000
+        w = dict(n=n, re=100.0, lid=1.0, dt=1e-3, tol=1e-6, itmax=1000000)
+        res, g = windows(w, steps, 100, sor_omega=1.5)
+        p = orc.make_params(n, re=100.0, dt=1e-3, tol=1e-6, beta=1.5, itmax=1000000, threads=1)
+        W, U, V, PSI = orc.initial_state(n)
+        t0 = time.perf_counter()
+        rc, info = orc.run(p, steps, W, U, V, PSI)
+        t1 = time.perf_counter()
+        res["bitwise_equal_to_oracle"] = all(np.array_equal(a.view(np.uint64), b.view(np.uint64))
+                                             for a, b in zip(g, (W, U, V, PSI)))
+        res["oracle_1_core"] = mcells(n * n, steps, (t1 - t0) * 1e3)
+        out["fp64"] = res
+    elif which == 2:
+        w = workload(1024)
+        out["workload"] = workload_name(w) + ", 10,000 steps"
+        fields = {}
+        for name, prec, ptype in (("fp64", 0, 2), ("mixed", 2, 2), ("direct", 0, 4)):
+            out[name], fields[name] = windows(w, 10000, 500, precision=prec, poisson_type=ptype)
+        for name in ("fp64", "mixed"):
+            out[name]["error_vs_converged_fp64"] = field_error(fields[name], fields["direct"])
+        out["mixed"]["error_vs_fp64_sor"] = field_error(fields["mixed"], fields["fp64"])
+    elif which == 3:
+        w = workload(2048)
+        init = dict(init_field=1, seed=2024, init_sigma=0.1, init_smooth_passes=8)
+        out["workload"] = f"2048x2048 cavity, Re 1000, lid 1, dt={w['dt']:.6g}, noise start, 5,000 steps"
+        fields = {}
+        forms = (("fp64", 0, 2),) if args.with_sor else ()
+        for name, prec, ptype in forms + (("mixed", 2, 2), ("direct", 0, 4)):
+            out[name], fields[name] = windows(w, 5000, 500, precision=prec, poisson_type=ptype, **init)
+        for name in fields:
+            if name != "direct":
+                out[name]["error_vs_converged_fp64"] = field_error(fields[name], fields["direct"])
+    elif which == 4:
+        steps = 2000
+        specs = cnvpy.batch_specs(256, seed=0)
+        base = cnvpy.default_config(mixed_rtol=1e-10)
+        sample = [next(k for k, x in enumerate(specs) if x["n"] == n) for n in sorted({x["n"] for x in specs})]
+        with cnvpy.Batch(base, specs) as bt:
+            bt.tune()
+            rows, total_ms = [], 0.0
+            for k in range(steps // 250):
+                rc, last = bt.step(250)
+                cells, _, ms = bt.stats()
+                total_ms += ms
+                rows.append({"steps": [250 * k, 250 * k + 249], "value": mcells(cells, 250, ms),
+                             "max_relative_residual": max(x["err"] for x in last)})
+            fields = {k: bt.get_fields(k) for k in sample}
+        errs = {}
+        for k in sample:
+            sp = specs[k]
+            h = 1.0 / sp["n"]
+            dt = sp["dt"] or 0.2 * min(h * h * sp["Re"] / 4.0, h / abs(sp["lid"]))
+            cfg = cnvpy.default_config(nx=sp["n"], ny=sp["n"], Re=sp["Re"], u4=sp["lid"], dt=dt, poisson_type=4)
+            with cnvpy.Cavity(cfg) as cav:
+                cav.step(steps)
+                errs[f"n{sp['n']}"] = field_error(fields[k], cav.get_fields())
+        out["batched"] = {"value": mcells(cells, steps, total_ms), "steps": steps, "cells": cells,
+                          "seconds": round(total_ms / 1e3, 2), "windows": rows, "error_vs_converged_fp64": errs}
+    print(json.dumps(out), flush=True)
+
+
 def only(args):
     """One small invocation of each named form, in order, for profilers: the kernels run as in the
     forms above; prints one JSON line of wall times (not a benchmark result)."""
@@ -638,9 +795,14 @@ def main():
     ap.add_argument("--only", default=None,
                     help="comma list of fp64,fp64_fma,mixed,direct,batched,adjoint (fp64@512: on a 512^2 "
                          "cavity): run one small case of each (for profilers) and exit")
+    ap.add_argument("--full-config", type=int, choices=[1, 2, 3, 4], default=None,
+                    help="run that workload to its stated step count and print its JSON line (minutes)")
+    ap.add_argument("--with-sor", action="store_true", help="--full-config 3: also the FP64 SOR path (~25 min)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)  # at least 3 untimed warm-up steps
-    if args.only:
+    if args.full_config:
+        full_config(args)
+    elif args.only:
         only(args)
     elif args.impl == "reference":
         reference(args)

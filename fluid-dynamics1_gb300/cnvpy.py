@@ -80,6 +80,7 @@ _SIGS = {
     "cnv_poisson": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(C.c_int), _dp]),
     "cnv_poisson_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), _dp]),
     "cnv_last_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), _dp, _dp]),
+    "cnv_time_passes": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp]),
     "cnv_solver_info": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "cnv_probe_fp64": (C.c_int, [C.c_int, _dp, _dp]),
     "cnv_check_mul_rn": (C.c_int, [C.c_int, _dp, C.c_int, C.c_double, _dp]),
@@ -242,6 +243,13 @@ class Cavity:
         it, err = C.c_int(0), C.c_double(0.0)
         rc = self._lib.cnv_poisson(self._h, _ptr(np.ascontiguousarray(f)), _ptr(psi), C.byref(it), C.byref(err))
         return rc, psi, it.value, err.value
+
+    def time_passes(self, reps: int = 20):
+        """(ms of the pre-solve pass, ms of the post-solve pass), mean over reps launches each
+        (cnv_time_passes)."""
+        pre, post = C.c_double(0), C.c_double(0)
+        check(self._lib.cnv_time_passes(self._h, reps, C.byref(pre), C.byref(post)), "cnv_time_passes")
+        return pre.value, post.value
 
     def solver_info(self) -> str:
         """The Poisson solver this cavity runs and its geometry (cnv_solver_info)."""

@@ -897,6 +897,28 @@ int cnv_solver_info(cnv_state* s, char* buf, size_t len) {
     return CNV_OK;
 }
 
+int cnv_time_passes(cnv_state* s, int reps, double* pre_ms, double* post_ms) {
+    if (!s || reps < 1) return fail(CNV_BAD_ARG, "null state or reps < 1");
+    CNV_CUDA(cudaSetDevice(s->device));
+    int rc = build_graphs(s);
+    if (rc != CNV_OK) return rc;
+    rc = reset_ctrl(s);
+    if (rc != CNV_OK) return rc;
+    const int parity = s->cur;
+    float ms[2] = {0, 0};
+    for (int pass = 0; pass < 2; ++pass) {
+        CNV_CUDA(cudaGraphLaunch(s->graph[pass][parity], s->stream));  // warm-up
+        CNV_CUDA(cudaEventRecord(s->ev0, s->stream));
+        for (int r = 0; r < reps; ++r) CNV_CUDA(cudaGraphLaunch(s->graph[pass][parity], s->stream));
+        CNV_CUDA(cudaEventRecord(s->ev1, s->stream));
+        CNV_CUDA(cudaEventSynchronize(s->ev1));
+        CNV_CUDA(cudaEventElapsedTime(&ms[pass], s->ev0, s->ev1));
+    }
+    if (pre_ms) *pre_ms = ms[0] / reps;
+    if (post_ms) *post_ms = ms[1] / reps;
+    return reset_ctrl(s) == CNV_OK ? check_guards(s) : CNV_CUDA_ERROR;
+}
+
 int cnv_last_stats(cnv_state* s, long long* sweeps, double* ms, double* poisson_ms) {
     if (!s) return fail(CNV_BAD_ARG, "null state");
     if (sweeps) *sweeps = s->last_sweeps;

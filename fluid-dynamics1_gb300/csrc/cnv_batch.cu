@@ -696,12 +696,18 @@ int group_size(int n, int smem_bytes, int split, int min_n) {
 
 // Estimated device time of one step of an n x n cavity on g blocks (microseconds): about 4n FP32
 // sweeps over n^2 cells at the measured per-SM rates (3.9 k cells/us with the correction in
-// shared memory, 1.5 k from L2), with the halo rows of a strip, plus the FP64 passes.
+// shared memory, 1.5 k from L2), with the halo rows of a strip, plus the FP64 passes; and for a
+// group, its barriers: one per 4 FP32 sweeps (the border-row swap) plus about 20 around the
+// residual norms and the passes, each about kBarrierUs (the wait for the slowest strip and the
+// halo rows' L2 round trip), which the strips cannot share out.
+constexpr double kBarrierUs = 3.5;
+
 double step_cost(int n, int g, int smem_mode) {
     const double cells = (double)n * n;
     const double rate = (g > 1 || smem_mode >= 1) ? 3.9e3 : 1.5e3;
     const double halo = g > 1 ? ((double)n / g + 2 * kStripHalo) / ((double)n / g) : 1.0;
-    return (4.0 * n * cells / rate * halo + 0.061 * cells) / g;
+    const double barriers = g > 1 ? kBarrierUs * (n + 20.0) : 0.0;
+    return (4.0 * n * cells / rate * halo + 0.061 * cells) / g + barriers;
 }
 
 int build_graph(cnv_batch* b) {
@@ -829,9 +835,10 @@ void assign_groups(std::vector<CavityDesc>& desc, int smem_bytes, int split, int
     }
 }
 
-// Smallest cavity that fits one block and that the cost model may still split: the model leaves
-// out the group barriers (about 4n/S + 20 per step), which only large cavities amortise.
-constexpr int kMinSplitN = 128;
+// Smallest cavity that fits one block and that the cost model may still split: two strips of at
+// least two halos each. The model weighs the group barriers, so it leaves small cavities whole
+// unless splitting them shortens the schedule.
+constexpr int kMinSplitN = 4 * kStripHalo;
 
 // Group sizes chosen by the cost model: each of the three largest distinct cavity sizes that
 // needs row strips, or fits one block and has at least kMinSplitN points, gets a group from the

@@ -291,6 +291,16 @@ int cnv_adjoint_stats(cnv_adjoint *a, double *forward_ms, double *backward_ms, l
  * the last step or solve it ran (ms). Any pointer may be NULL. */
 int cnv_last_stats(cnv_state *s, long long *sweeps, double *ms, double *poisson_ms);
 
+/* Device time of the step's two passes around the Poisson solve, for measurement: the
+ * pre-solve pass (wall vorticity, derivatives, Euler update, right-hand side) and the
+ * post-solve pass (velocity, continuity) are each replayed reps times on the state's current
+ * fields, and the mean ms per launch of each is returned (CUDA events on the state's stream).
+ * Both passes are idempotent on the fields they read: afterwards the edge cells of w hold the
+ * wall vorticity the next step's first pass gives them anyway, every other field is unchanged,
+ * and the next cnv_step gives the same results as without this call. No counterpart in the
+ * reference. */
+int cnv_time_passes(cnv_state *s, int reps, double *pre_ms, double *post_ms);
+
 /* One line naming the Poisson solver this state runs and its geometry, e.g.
  * "sor-exchange grid=304 tiles=16x19" (FP64 SOR/GS exchanging every half-sweep),
  * "sor-tiled sweeps=4 grid=150 tiles=5x30", "mixed grid=152 tiles=8x19" or

@@ -38,6 +38,16 @@ def test_plan_of_the_256_cavity_workload(cnv):
     assert 30e3 < us < 36e3, us  # measured on a GB300: 33.5 ms per step
 
 
+def test_plan_of_ten_192_cavities_counts_the_group_barriers(cnv):
+    """Ten 192^2 cavities: the plan splits each into row strips, and its estimate includes the
+    groups' barriers (one per 4 FP32 sweeps plus about 20 per step). Measured on a GB300: 3.9 ms
+    per step on 4-strip groups (9.8 ms on one block each); without the barrier term the estimate
+    was 3.0 ms. It must be within 10% now."""
+    groups, us = cnv.batch_plan([dict(n=192, Re=1000.0, lid=1.0)] * 10)
+    assert len(set(groups)) == 1 and groups[0] >= 2, groups
+    assert abs(us - 3.9e3) <= 0.1 * 3.9e3, us
+
+
 def test_plan_balances_a_few_large_cavities_and_rejects_bad_input(cnv):
     # three cavities on 152 blocks: more strips than needed shorten the step
     groups, us = cnv.batch_plan([dict(n=384, Re=1500.0, lid=1.2), dict(n=256, Re=300.0, lid=0.7),
