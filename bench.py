@@ -540,12 +540,11 @@ def ours(args):
     peak, peak_kind = measured_peaks()
     traffic = POISSON_TRAFFIC["bytes_per_launch"] if args.form == "fp64" else None
     fp64 = None
-    add_mul = cnvpy.probe_fp64(local)[0]
+    add_mul, fma_rate = cnvpy.probe_fp64(local)
     if args.form == "fp64":
         # the binding ceiling: the update's 7 FP64 add/multiply operations per interior cell-sweep
         # (5 on the FP64 pipe, the 2 multiplications by constants in exact integer arithmetic),
         # against the device's own FP64 rate for that mix (probe kernels, same process)
-        fma_rate = cnvpy.probe_fp64(local)[1]
         ops = 7.0 * interior * sweeps / (pms * 1e-3)
         fp64 = {"achieved_gops": round(ops / 1e9, 1), "peak_gops": round(add_mul / 1e9, 1),
                 "frac": round(ops / add_mul, 4), "fma_peak_gops": round(fma_rate / 1e9, 1),

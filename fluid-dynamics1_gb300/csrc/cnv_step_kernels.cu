@@ -263,16 +263,21 @@ __global__ void __launch_bounds__(kStepThreads) k_post(StepArgs a, int continuit
         last = (t == gridDim.x - 1);
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return;
-    // last block: fold the partials, write this step's record, re-arm the barrier and ticket
+    if (!last || warp != 0) return;
+    // last block, first warp: fold the partials (each lane a stride of blocks, L2 loads issued
+    // together), write this step's record, re-arm the barrier and ticket
     __threadfence();
-    const volatile double* cp = a.cont_partials;
+    const double* cp = a.cont_partials;
     mx = Ext{-DBL_MAX, -1};
     mn = Ext{DBL_MAX, -1};
-    for (int q = 0; q < (int)gridDim.x; ++q) {
-        take_max(mx, cp[4 * q], (int)cp[4 * q + 1]);
-        take_min(mn, cp[4 * q + 2], (int)cp[4 * q + 3]);
+    for (int q = lane; q < (int)gridDim.x; q += 32) {
+        const double2 hi = __ldcg(reinterpret_cast<const double2*>(cp + 4 * q));
+        const double2 lo = __ldcg(reinterpret_cast<const double2*>(cp + 4 * q + 2));
+        take_max(mx, hi.x, (int)hi.y);
+        take_min(mn, lo.x, (int)lo.y);
     }
+    warp_ext(mx, mn);
+    if (lane != 0) return;
     ctl->cont_ticket = 0;
     ctl->bar_count = 0;  // every block passed the barrier before taking its ticket
     const int step = ctl->step;
