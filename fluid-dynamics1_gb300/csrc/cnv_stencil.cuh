@@ -25,28 +25,39 @@ __device__ __forceinline__ double vel_bc(const double* f, int n, int i, int j, d
     return f[(size_t)i * n + j];
 }
 
+// c * x rounded to nearest: on the FP64 pipe, or (MUL == kMulInt) by the exact integer multiply
+// of cnv_sor.cuh where it applies (the same bits either way). A translation unit that uses kMulInt
+// specialises band_mul<kMulInt> after including cnv_sor.cuh.
+enum MulPipe { kMulFp64 = 0, kMulInt = 1 };
+template <int MUL>
+__device__ __forceinline__ double band_mul(double c, double x);
+template <>
+__device__ __forceinline__ double band_mul<kMulFp64>(double c, double x) {
+    return dmul(c, x);
+}
+
 // sum over offsets o of band[class(j)][o] * x(i, j+o), ascending column (DX-type product)
-template <class Load>
+template <int MUL = kMulFp64, class Load>
 __device__ __forceinline__ double along_j(const double (*band)[kTaps], int n, int i, int j, Load x) {
     const double* c = band[row_class(j, n)];
     double acc = 0.0;
 #pragma unroll
     for (int o = -3; o <= 3; ++o) {
         const int col = j + o;
-        if (col >= 0 && col < n) acc = dadd(acc, dmul(c[o + 3], x(i, col)));
+        if (col >= 0 && col < n) acc = dadd(acc, band_mul<MUL>(c[o + 3], x(i, col)));
     }
     return acc;
 }
 
 // sum over offsets o of band[class(i)][o] * x(i+o, j), ascending row (DY-type product)
-template <class Load>
+template <int MUL = kMulFp64, class Load>
 __device__ __forceinline__ double along_i(const double (*band)[kTaps], int n, int i, int j, Load x) {
     const double* c = band[row_class(i, n)];
     double acc = 0.0;
 #pragma unroll
     for (int o = -3; o <= 3; ++o) {
         const int row = i + o;
-        if (row >= 0 && row < n) acc = dadd(acc, dmul(c[o + 3], x(row, j)));
+        if (row >= 0 && row < n) acc = dadd(acc, band_mul<MUL>(c[o + 3], x(row, j)));
     }
     return acc;
 }

@@ -34,11 +34,26 @@
 #include <climits>
 
 #include "cnv_kernels.h"
+#include "cnv_sor.cuh"
 #include "cnv_stencil.cuh"
 #include "cnv_sync.cuh"
 
 namespace cnv {
+
+template <>
+__device__ __forceinline__ double band_mul<kMulInt>(double c, double x) {
+    return mul_rn(c, x);
+}
+
 namespace {
+
+// Which pipe multiplies the band coefficients in the passes' derivative products: the passes are
+// bound by the FP64 pipe, and the exact integer multiply can move part of that work to the
+// integer pipes (the same bits).
+constexpr int kPreD1 = kMulFp64;     // k_pre: DX w, DY w
+constexpr int kPreD2 = kMulFp64;     // k_pre: DX2 w, DY2 w
+constexpr int kPostVel = kMulFp64;   // k_post: DY psi, DX psi
+constexpr int kPostCont = kMulFp64;  // k_post: DX u, DY v
 
 constexpr int kTX = 32;                 // tile columns (one warp across)
 constexpr int kTY = 32;                 // tile rows
@@ -108,10 +123,10 @@ __global__ void __launch_bounds__(kStepThreads) k_pre(StepArgs a) {
     for (int k = 0; k < kRowsPerThread; ++k) {
         const int i = i0 + ty + k * (kStepThreads / kTX);
         if (i >= n) break;
-        const double wx = along_j(sb.d1x, n, i, j, W);   // dwdx   = DX  w
-        const double wy = along_i(sb.d1y, n, i, j, W);   // dwdy   = DY  w
-        const double wxx = along_j(sb.d2x, n, i, j, W);  // d2wdx2 = DX2 w
-        const double wyy = along_i(sb.d2y, n, i, j, W);  // d2wdy2 = DY2 w
+        const double wx = along_j<kPreD1>(sb.d1x, n, i, j, W);   // dwdx   = DX  w
+        const double wy = along_i<kPreD1>(sb.d1y, n, i, j, W);   // dwdy   = DY  w
+        const double wxx = along_j<kPreD2>(sb.d2x, n, i, j, W);  // d2wdx2 = DX2 w
+        const double wyy = along_i<kPreD2>(sb.d2y, n, i, j, W);  // d2wdy2 = DY2 w
         const double ue = vel_bc(a.u, n, i, j, bc.u1, bc.u2, bc.u3, bc.u4);
         const double ve = vel_bc(a.v, n, i, j, bc.v1, bc.v2, bc.v3, bc.v4);
         const double w0 = W(i, j);
@@ -186,8 +201,8 @@ __global__ void __launch_bounds__(kStepThreads) k_post(StepArgs a, int continuit
             for (int k = 0; k < kRowsPerThread; ++k) {
                 const int i = i0 + ty + k * (kStepThreads / kTX);
                 if (i >= n) break;
-                const double uu = along_i(sb.d1y, n, i, j, P);   // DY psi
-                const double vv = -along_j(sb.d1x, n, i, j, P);  // -(DX psi)
+                const double uu = along_i<kPostVel>(sb.d1y, n, i, j, P);   // DY psi
+                const double vv = -along_j<kPostVel>(sb.d1x, n, i, j, P);  // -(DX psi)
                 const size_t at = (size_t)i * n + j;
                 a.u[at] = uu;
                 a.v[at] = vv;
@@ -230,8 +245,8 @@ __global__ void __launch_bounds__(kStepThreads) k_post(StepArgs a, int continuit
             for (int k = 0; k < kRowsPerThread; ++k) {
                 const int i = i0 + ty + k * (kStepThreads / kTX);
                 if (i >= n) break;
-                const double dudx = along_j(sb.d1x, n, i, j, U);
-                const double dvdy = along_i(sb.d1y, n, i, j, V);
+                const double dudx = along_j<kPostCont>(sb.d1x, n, i, j, U);
+                const double dvdy = along_i<kPostCont>(sb.d1y, n, i, j, V);
                 const double c = dadd(dudx, dvdy);
                 take_max(mx, c, i * n + j);
                 take_min(mn, c, i * n + j);
