@@ -23,18 +23,20 @@
 // solve is the same call. The differentiable form uses it: a finite-difference check of the
 // gradient needs a solve far tighter than an iterative stop rule gives.
 //
-// The row transforms. A DST-I of length m is the DFT of length len = 2(m+1) of
-// the row's odd extension (0, x_0 .. x_{m-1}, 0, -x_{m-1} .. -x_0): the DFT is -2i times the
-// unnormalised DST. Two rows go into one complex sequence (row a as its real part, row b as its
-// imaginary part); the DFT of that sequence is -2i DST(a) + 2 DST(b), so one complex FFT gives
-// both rows. The FFT is a mixed-radix Stockham transform (self-sorting, two shared-memory
-// buffers, one block per row pair) over the prime factors p of len: each stage applies the
-// twiddles, then a p-point DFT in its symmetric form (for odd p, outputs q and p-q share the
-// sums over u_q + u_{p-q} and u_q - u_{p-q}: 2(p-1) multiply-adds per output pair). Per row
-// that is about len * (sum of the radices) multiply-adds, against m^2 / 2 for a dense product:
-// at n = 1024 (len = 2046 = 2 * 3 * 11 * 31) about 10 times fewer FP64 operations. Grids whose
-// len has a prime factor above kMaxRadix, or that do not fit shared memory, take the dense
-// products with S instead (each folded by the mirror symmetry S[b][m-1-c] = (-1)^b S[b][c]).
+// The row transforms. The DST-I F_k = sum_j y_j sin(pi j k / N) of a row y_1 .. y_{N-1} (N = m+1)
+// comes from the real DFT of length N of w_j = sin(pi j / N)(y_j + y_{N-j}) + (y_j - y_{N-j})/2: with
+// C_k + i S_k = sum_j w_j exp(2 pi i j k / N), the even outputs are F_2k = S_k and the odd ones
+// follow from F_2k+1 = F_2k-1 + C_k, F_1 = C_0 / 2, a prefix sum (the method of Numerical Recipes'
+// sinft, which works for any N). Two rows go into one complex sequence (real and imaginary parts)
+// and are separated after the FFT by the conjugate symmetry of real transforms. The FFT is a
+// mixed-radix Stockham transform (self-sorting, two shared-memory buffers, one block per row pair)
+// over the prime factors p of N: each stage applies the twiddles, then a p-point DFT in its
+// symmetric form (for odd p, outputs q and p-q share the sums over u_q + u_{p-q} and u_q - u_{p-q}:
+// 2(p-1) multiply-adds per output pair). Per row that is about N/2 * (sum of the radices + 9)
+// FP64 operations, against m^2 / 2 for a dense product: at n = 1024 (N = 1023 = 3 * 11 * 31)
+// about a twentieth. Grids whose N has a prime factor above kMaxRadix, or that do not fit shared
+// memory, take the dense products with S instead (each folded by the mirror symmetry
+// S[b][m-1-c] = (-1)^b S[b][c]).
 #include <cmath>
 #include <vector>
 
@@ -44,16 +46,17 @@ namespace cnv {
 namespace {
 
 // ---------------------------------------------------------------- FFT row transforms
-constexpr int kFftThreads = 512;
+constexpr int kFftThreads = 256;
 
 struct FftArgs {
-    int m, len, nstages;
+    int m, len, nstages;       // len = N = m + 1
     int radix[kMaxFftStages];
     int csoff[kMaxFftStages];  // offset of each stage's p-point table in cs
     int ncs;
-    const double2* tw;         // exp(-2 pi i t / len), t = 0 .. len-1
+    const double2* tw;         // exp(-2 pi i t / N), t = 0 .. N-1
     const double2* cs;         // per stage: (cos 2 pi t / p, sin 2 pi t / p), t = 0 .. p-1
-    double norm;               // 1 / sqrt(2 (m+1)): orthonormal DST from the DFT
+    const double* sn;          // sin(pi j / N), j = 0 .. N-1
+    double norm;               // sqrt(2 / N): the orthonormal DST
 };
 
 // Destination of a transform's value for row r, column c: row-major out[(r + off) * ld + c + off],
@@ -86,7 +89,7 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 }
 
 // Orthonormal DST-I of rows 2*blockIdx.x and 2*blockIdx.x + 1 of X(r, c) = xs * x[(r + xo) * xld
-// + c + xo] (r, c < m), written to dst.
+// + c + xo] (r, c < m), written to dst. T's first 2(K+1) doubles hold the C_k after the FFT.
 __global__ void __launch_bounds__(kFftThreads) k_dst_fft(FftArgs F, const double* __restrict__ x, int xld, int xo,
                                                           double xs, DstDest dst) {
     extern __shared__ double2 fsm[];
@@ -98,20 +101,16 @@ __global__ void __launch_bounds__(kFftThreads) k_dst_fft(FftArgs F, const double
     for (int t = threadIdx.x; t < F.ncs; t += kFftThreads) CS[t] = F.cs[t];
     const double* xa = x + (size_t)(ra + xo) * xld + xo;
     const double* xb = x + (size_t)(rb + xo) * xld + xo;
-    for (int t = threadIdx.x; t < len; t += kFftThreads) {
-        // odd extension: 0, x_0 .. x_{m-1}, 0, -x_{m-1} .. -x_0
-        double a = 0.0, b = 0.0;
-        if (t != 0 && t != m + 1) {
-            const bool lo = t <= m;
-            const int c = lo ? t - 1 : len - t - 1;
-            a = xs * __ldg(xa + c);
-            b = rb < m ? xs * __ldg(xb + c) : 0.0;
-            if (!lo) {
-                a = -a;
-                b = -b;
-            }
-        }
-        X[t] = make_double2(a, b);
+    const bool two = rb < m;
+    for (int j = threadIdx.x; j < len; j += kFftThreads) {
+        // w_j = sin(pi j / N)(y_j + y_{N-j}) + (y_j - y_{N-j})/2 with y_j = X(row, j - 1); for
+        // j = 0 both y_0 and y_N lie outside 1 .. m and are 0, for j >= 1 both lie inside
+        const int jn = len - j;
+        const bool in = j >= 1;
+        const double s = __ldg(F.sn + j);
+        const double a1 = in ? xs * __ldg(xa + j - 1) : 0.0, a2 = in ? xs * __ldg(xa + jn - 1) : 0.0;
+        const double b1 = (two && in) ? xs * __ldg(xb + j - 1) : 0.0, b2 = (two && in) ? xs * __ldg(xb + jn - 1) : 0.0;
+        X[j] = make_double2(__fma_rn(s, a1 + a2, 0.5 * (a1 - a2)), __fma_rn(s, b1 + b2, 0.5 * (b1 - b2)));
     }
     __syncthreads();
     int L = 1;  // length of the sub-transforms done so far
@@ -189,11 +188,41 @@ __global__ void __launch_bounds__(kFftThreads) k_dst_fft(FftArgs F, const double
         }
         L = Lp;
     }
-    // bins 1 .. m: DFT = -2i DST(a) + 2 DST(b)
-    for (int k = 1 + threadIdx.x; k <= m; k += kFftThreads) {
-        const double2 W = X[k];
-        dst.put(ra, k - 1, -W.y * F.norm);
-        if (rb < m) dst.put(rb, k - 1, W.x * F.norm);
+    // separate the two real transforms: X_a(k) = (Z_k + conj Z_{N-k}) / 2, X_b(k) = (Z_k - conj Z_{N-k}) / 2i,
+    // and with X(k) = C_k - i S_k (forward FFT): the even outputs F_2k = S_k; C_k kept for the odd ones
+    const int K = len / 2;
+    double* const Cs = reinterpret_cast<double*>(T);  // C of row a at Cs[k], of row b at Cs[K + 1 + k]
+    for (int k = threadIdx.x; k <= K; k += kFftThreads) {
+        const double2 zk = X[k], zc = X[k ? len - k : 0];
+        Cs[k] = 0.5 * (zk.x + zc.x);
+        Cs[K + 1 + k] = 0.5 * (zk.y + zc.y);
+        if (k >= 1 && 2 * k <= m) {
+            dst.put(ra, 2 * k - 1, -0.5 * (zk.y - zc.y) * F.norm);
+            if (two) dst.put(rb, 2 * k - 1, 0.5 * (zk.x - zc.x) * F.norm);
+        }
+    }
+    __syncthreads();
+    // odd outputs F_2k+1 = C_0/2 + C_1 + ... + C_k: a prefix sum, row a by warp 0, row b by warp 1
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp > 1 || (warp == 1 && !two)) return;
+    const double* C = Cs + warp * (K + 1);
+    const int row = warp ? rb : ra;
+    const int count = (m + 1) / 2;  // odd outputs 1, 3, .. <= m
+    const int chunk = (count + 31) / 32;
+    const int k0 = min(count, lane * chunk), k1 = min(count, k0 + chunk);
+    double own = 0.0;
+    for (int k = k0; k < k1; ++k) own += C[k];
+    double incl = own;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const double v = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += v;
+    }
+    double acc = incl - own;  // the sum over the lanes before this one
+    const double half0 = 0.5 * C[0];
+    for (int k = k0; k < k1; ++k) {
+        acc += C[k];
+        dst.put(row, 2 * k, (acc - half0) * F.norm);
     }
 }
 
@@ -266,7 +295,8 @@ FftArgs fft_args(const DstPlan& P) {
     F.ncs = P.ncs;
     F.tw = P.tw;
     F.cs = P.cs;
-    F.norm = 1.0 / std::sqrt(2.0 * (P.m + 1));
+    F.sn = P.sn;
+    F.norm = std::sqrt(2.0 / (P.m + 1));
     return F;
 }
 
@@ -334,8 +364,8 @@ int dst_plan_create(int n, double dx, double dy, DstPlan* P) {
     cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 
-    // the FFT row transforms where len = 2(m+1) factors into small primes and fits shared memory
-    const int len = 2 * (m + 1);
+    // the FFT row transforms where N = m+1 factors into small primes and fits shared memory
+    const int len = m + 1;
     int radix[kMaxFftStages], ns = 0;
     if (factor(len, radix, &ns)) {
         int ncs = 0;
@@ -346,12 +376,14 @@ int dst_plan_create(int n, double dx, double dy, DstPlan* P) {
             P->nstages = ns;
             P->ncs = ncs;
             P->fft_smem = (int)smem;
-            std::vector<double2> tw(len), cs(ncs);
             // tables in long double, rounded once to double
             const long double lpi = 3.141592653589793238462643383279502884L;
+            std::vector<double2> tw(len), cs(ncs);
+            std::vector<double> sn(len);
             for (int t = 0; t < len; ++t) {
-                const long double a = 2 * lpi * t / len;  // exp(-2 pi i t / len)
+                const long double a = 2 * lpi * t / len;  // exp(-2 pi i t / N)
                 tw[t] = make_double2((double)std::cos(a), (double)-std::sin(a));
+                sn[t] = (double)std::sin(lpi * t / len);
             }
             for (int s = 0, off = 0; s < ns; ++s) {
                 P->radix[s] = radix[s];
@@ -364,8 +396,10 @@ int dst_plan_create(int n, double dx, double dy, DstPlan* P) {
             }
             if (cudaMalloc(&P->tw, len * sizeof(double2)) != cudaSuccess ||
                 cudaMalloc(&P->cs, ncs * sizeof(double2)) != cudaSuccess ||
+                cudaMalloc(&P->sn, len * sizeof(double)) != cudaSuccess ||
                 cudaMemcpy(P->tw, tw.data(), len * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
                 cudaMemcpy(P->cs, cs.data(), ncs * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemcpy(P->sn, sn.data(), len * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
                 cudaFuncSetAttribute(k_dst_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, P->fft_smem) !=
                     cudaSuccess) {
                 dst_plan_destroy(P);
@@ -418,6 +452,7 @@ void dst_plan_destroy(DstPlan* P) {
     cudaFree(P->lam_j);
     cudaFree(P->tw);
     cudaFree(P->cs);
+    cudaFree(P->sn);
     *P = DstPlan{};
 }
 

@@ -8,21 +8,22 @@
 namespace cnv {
 
 constexpr int kMaxFftStages = 24;  // prime factors of the FFT length
-constexpr int kMaxRadix = 251;     // largest prime factor the FFT row transform takes
+constexpr int kMaxRadix = 251;     // largest prime factor of n - 1 the FFT row transform takes
 
 struct DstPlan {
     int n = 0, m = 0;          // grid size and interior size m = n - 2
     double den = 0;            // 2 (dx^2 + dy^2)
     double dx2 = 0, dy2 = 0;
-    // FFT row transforms (len = 2 (m+1) > 0), else dense products with S
+    // FFT row transforms (len = N = m + 1 > 0), else dense products with S
     int len = 0;
     int nstages = 0;
     int radix[kMaxFftStages] = {};
     int csoff[kMaxFftStages] = {};
     int ncs = 0;
     int fft_smem = 0;          // dynamic shared memory of the FFT kernel
-    double2* tw = nullptr;     // exp(-2 pi i t / len)
+    double2* tw = nullptr;     // exp(-2 pi i t / N)
     double2* cs = nullptr;     // per stage: (cos, sin)(2 pi t / p)
+    double* sn = nullptr;      // sin(pi j / N)
     int rows = 4;              // rows per block of the dense product kernel
     double* S = nullptr;       // m x m orthonormal DST-I matrix (symmetric), dense path only
     double* lam_i = nullptr;   // 4 dy^2 sin^2(pi (a+1) / (2 (m+1))): the eigenvalue part along i

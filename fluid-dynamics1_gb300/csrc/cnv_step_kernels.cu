@@ -48,12 +48,14 @@ __device__ __forceinline__ double band_mul<kMulInt>(double c, double x) {
 namespace {
 
 // Which pipe multiplies the band coefficients in the passes' derivative products: the passes are
-// bound by the FP64 pipe, and the exact integer multiply can move part of that work to the
-// integer pipes (the same bits).
+// bound by the FP64 pipe, and the exact integer multiply moves part of that work to the integer
+// pipes (the same bits). Measured on a GB300 (cnv_time_passes, ms at 1024^2 / 2048^2): k_post
+// 0.168 / 0.644 with FP64 multiplies, 0.164 / 0.446 with all 28 on the integer pipes; k_pre
+// 0.162 / 0.544 either way (it gains nothing), so it keeps the FP64 pipe.
 constexpr int kPreD1 = kMulFp64;     // k_pre: DX w, DY w
 constexpr int kPreD2 = kMulFp64;     // k_pre: DX2 w, DY2 w
-constexpr int kPostVel = kMulFp64;   // k_post: DY psi, DX psi
-constexpr int kPostCont = kMulFp64;  // k_post: DX u, DY v
+constexpr int kPostVel = kMulInt;    // k_post: DY psi, DX psi
+constexpr int kPostCont = kMulInt;   // k_post: DX u, DY v
 
 constexpr int kTX = 32;                 // tile columns (one warp across)
 constexpr int kTY = 32;                 // tile rows
