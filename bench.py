@@ -759,11 +759,13 @@ def only(args):
     out = {}
     for item in args.only.split(","):
         name, _, size = item.partition("@")  # e.g. fp64@512: that form on a 512^2 cavity
+        size, _, start = size.partition("+")  # direct@2048+noise: from a smoothed-noise vorticity
+        init = dict(init_field=1, seed=2024, init_sigma=0.1, init_smooth_passes=8) if start == "noise" else {}
         t0 = time.perf_counter()
         if name in ("fp64", "fp64_fma", "mixed", "direct"):
             prec, ptype, _ = FORMS[name]
             run_device(cnvpy, workload(int(size) if size else 1024), 0, 1, 0, lambda: None, precision=prec,
-                       poisson_type=ptype)
+                       poisson_type=ptype, **init)
         elif name == "batched":
             with cnvpy.Batch(cnvpy.default_config(mixed_rtol=1e-10), cnvpy.batch_specs(256, seed=0)) as bt:
                 bt.tune()  # one launch per candidate decomposition (5), then the step on the kept one
@@ -793,7 +795,8 @@ def main():
                     help="form measured for the headline value")
     ap.add_argument("--only", default=None,
                     help="comma list of fp64,fp64_fma,mixed,direct,batched,adjoint (fp64@512: on a 512^2 "
-                         "cavity): run one small case of each (for profilers) and exit")
+                         "cavity; direct@2048+noise: from a smoothed-noise vorticity): run one small case of "
+                         "each (for profilers) and exit")
     ap.add_argument("--full-config", type=int, choices=[1, 2, 3, 4], default=None,
                     help="run that workload to its stated step count and print its JSON line (minutes)")
     ap.add_argument("--with-sor", action="store_true", help="--full-config 3: also the FP64 SOR path (~25 min)")

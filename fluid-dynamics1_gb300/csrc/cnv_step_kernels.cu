@@ -48,12 +48,12 @@ __device__ __forceinline__ double band_mul<kMulInt>(double c, double x) {
 namespace {
 
 // Which pipe multiplies the band coefficients in the passes' derivative products: the passes are
-// bound by the FP64 pipe, and the exact integer multiply moves part of that work to the integer
-// pipes (the same bits). Measured on a GB300 (cnv_time_passes, ms at 1024^2 / 2048^2): k_post
-// 0.168 / 0.644 with FP64 multiplies, 0.164 / 0.446 with all 28 on the integer pipes; k_pre
-// 0.162 / 0.544 either way (it gains nothing), so it keeps the FP64 pipe.
-constexpr int kPreD1 = kMulFp64;     // k_pre: DX w, DY w
-constexpr int kPreD2 = kMulFp64;     // k_pre: DX2 w, DY2 w
+// bound by the FP64 pipe, and the exact integer multiply moves those multiplications to the
+// integer pipes (the same bits). Measured on a GB300 (cnv_time_passes on a developed, smoothed-
+// noise field; ms at 1024^2 / 2048^2): k_pre 0.162 / 0.544 with FP64 multiplies, 0.116 / 0.388
+// with all 28 on the integer pipes; k_post 0.168 / 0.643 and 0.166 / 0.446.
+constexpr int kPreD1 = kMulInt;      // k_pre: DX w, DY w
+constexpr int kPreD2 = kMulInt;      // k_pre: DX2 w, DY2 w
 constexpr int kPostVel = kMulInt;    // k_post: DY psi, DX psi
 constexpr int kPostCont = kMulInt;   // k_post: DX u, DY v
 
