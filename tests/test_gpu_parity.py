@@ -359,6 +359,25 @@ def test_nonfinite_input_rejected(cnv):
         assert rc == 0
 
 
+def test_time_passes_leaves_the_next_step_unchanged(cnv):
+    """cnv_time_passes replays the pre- and post-solve passes on the current fields; the following
+    step must give the same bits as without that call."""
+    out = []
+    for timed in (False, True):
+        cfg = make_cfg(cnv, 96, poisson_tol=1e-6)
+        with cnv.Cavity(cfg) as cav:
+            cav.step(2)
+            if timed:
+                pre_ms, post_ms = cav.time_passes(5)
+                assert pre_ms > 0 and post_ms > 0
+            rc, info = cav.step(2)
+            assert rc == 0
+            out.append(([s["iters"] for s in info], cav.get_fields()))
+    assert out[0][0] == out[1][0]
+    for name, a, b in zip("w u v psi".split(), out[0][1], out[1][1]):
+        assert bitwise(a, b), name
+
+
 def test_step_rows_matches_step(cnv):
     n = 20
     cfg = make_cfg(cnv, n)
