@@ -88,28 +88,22 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return make_double2(__fma_rn(a.x, b.x, -a.y * b.y), __fma_rn(a.x, b.y, a.y * b.x));
 }
 
-// Orthonormal DST-I of rows 2*blockIdx.x and 2*blockIdx.x + 1 of X(r, c) = xs * x[(r + xo) * xld
-// + c + xo] (r, c < m), written to dst. T's first 2(K+1) doubles hold the C_k after the FFT.
-__global__ void __launch_bounds__(kFftThreads) k_dst_fft(FftArgs F, const double* __restrict__ x, int xld, int xo,
-                                                          double xs, DstDest dst) {
-    extern __shared__ double2 fsm[];
-    double2* X = fsm;               // the sequence between stages
-    double2* T = fsm + F.len;       // a stage's twiddled (and for odd p, paired) inputs
-    double2* CS = fsm + 2 * F.len;  // the stages' p-point tables
+// Orthonormal DST-I of two rows (a and b; b absent when two is false), read through
+// load(row, c) (row 0 = a, 1 = b; c = 0 .. m-1) and written through store(row, c, value). X and T
+// are the two N-long complex buffers, CS the stages' tables in shared memory. T's first 2(K+1)
+// doubles hold the C_k after the FFT. Ends with a block barrier.
+template <class Load, class Store>
+__device__ __forceinline__ void dst_row_pair(const FftArgs& F, double2* X, double2* T, const double2* CS, bool two,
+                                             Load load, Store store) {
     const int m = F.m, len = F.len;
-    const int ra = 2 * blockIdx.x, rb = ra + 1;  // rb == m: no second row
-    for (int t = threadIdx.x; t < F.ncs; t += kFftThreads) CS[t] = F.cs[t];
-    const double* xa = x + (size_t)(ra + xo) * xld + xo;
-    const double* xb = x + (size_t)(rb + xo) * xld + xo;
-    const bool two = rb < m;
     for (int j = threadIdx.x; j < len; j += kFftThreads) {
         // w_j = sin(pi j / N)(y_j + y_{N-j}) + (y_j - y_{N-j})/2 with y_j = X(row, j - 1); for
         // j = 0 both y_0 and y_N lie outside 1 .. m and are 0, for j >= 1 both lie inside
         const int jn = len - j;
         const bool in = j >= 1;
         const double s = __ldg(F.sn + j);
-        const double a1 = in ? xs * __ldg(xa + j - 1) : 0.0, a2 = in ? xs * __ldg(xa + jn - 1) : 0.0;
-        const double b1 = (two && in) ? xs * __ldg(xb + j - 1) : 0.0, b2 = (two && in) ? xs * __ldg(xb + jn - 1) : 0.0;
+        const double a1 = in ? load(0, j - 1) : 0.0, a2 = in ? load(0, jn - 1) : 0.0;
+        const double b1 = (two && in) ? load(1, j - 1) : 0.0, b2 = (two && in) ? load(1, jn - 1) : 0.0;
         X[j] = make_double2(__fma_rn(s, a1 + a2, 0.5 * (a1 - a2)), __fma_rn(s, b1 + b2, 0.5 * (b1 - b2)));
     }
     __syncthreads();
@@ -197,33 +191,75 @@ __global__ void __launch_bounds__(kFftThreads) k_dst_fft(FftArgs F, const double
         Cs[k] = 0.5 * (zk.x + zc.x);
         Cs[K + 1 + k] = 0.5 * (zk.y + zc.y);
         if (k >= 1 && 2 * k <= m) {
-            dst.put(ra, 2 * k - 1, -0.5 * (zk.y - zc.y) * F.norm);
-            if (two) dst.put(rb, 2 * k - 1, 0.5 * (zk.x - zc.x) * F.norm);
+            store(0, 2 * k - 1, -0.5 * (zk.y - zc.y) * F.norm);
+            if (two) store(1, 2 * k - 1, 0.5 * (zk.x - zc.x) * F.norm);
         }
     }
     __syncthreads();
     // odd outputs F_2k+1 = C_0/2 + C_1 + ... + C_k: a prefix sum, row a by warp 0, row b by warp 1
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp > 1 || (warp == 1 && !two)) return;
-    const double* C = Cs + warp * (K + 1);
-    const int row = warp ? rb : ra;
-    const int count = (m + 1) / 2;  // odd outputs 1, 3, .. <= m
-    const int chunk = (count + 31) / 32;
-    const int k0 = min(count, lane * chunk), k1 = min(count, k0 + chunk);
-    double own = 0.0;
-    for (int k = k0; k < k1; ++k) own += C[k];
-    double incl = own;
+    if (warp == 0 || (warp == 1 && two)) {
+        const double* C = Cs + warp * (K + 1);
+        const int count = (m + 1) / 2;  // odd outputs 1, 3, .. <= m
+        const int chunk = (count + 31) / 32;
+        const int k0 = min(count, lane * chunk), k1 = min(count, k0 + chunk);
+        double own = 0.0;
+        for (int k = k0; k < k1; ++k) own += C[k];
+        double incl = own;
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        const double v = __shfl_up_sync(0xffffffffu, incl, off);
-        if (lane >= off) incl += v;
+        for (int off = 1; off < 32; off <<= 1) {
+            const double v = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += v;
+        }
+        double acc = incl - own;  // the sum over the lanes before this one
+        const double half0 = 0.5 * C[0];
+        for (int k = k0; k < k1; ++k) {
+            acc += C[k];
+            store(warp, 2 * k, (acc - half0) * F.norm);
+        }
     }
-    double acc = incl - own;  // the sum over the lanes before this one
-    const double half0 = 0.5 * C[0];
-    for (int k = k0; k < k1; ++k) {
-        acc += C[k];
-        dst.put(row, 2 * k, (acc - half0) * F.norm);
-    }
+    __syncthreads();
+}
+
+// Orthonormal DST-I of rows 2*blockIdx.x and 2*blockIdx.x + 1 of X(r, c) = xs * x[(r + xo) * xld
+// + c + xo] (r, c < m), written to dst.
+__global__ void __launch_bounds__(kFftThreads) k_dst_fft(FftArgs F, const double* __restrict__ x, int xld, int xo,
+                                                          double xs, DstDest dst) {
+    extern __shared__ double2 fsm[];
+    double2* X = fsm;               // the sequence between stages
+    double2* T = fsm + F.len;       // a stage's twiddled (and for odd p, paired) inputs
+    double2* CS = fsm + 2 * F.len;  // the stages' p-point tables
+    const int ra = 2 * blockIdx.x, rb = ra + 1;  // rb == m: no second row
+    for (int t = threadIdx.x; t < F.ncs; t += kFftThreads) CS[t] = F.cs[t];
+    const double* xr[2] = {x + (size_t)(ra + xo) * xld + xo, x + (size_t)(rb + xo) * xld + xo};
+    dst_row_pair(
+        F, X, T, CS, rb < F.m, [&](int row, int c) { return xs * __ldg(xr[row] + c); },
+        [&](int row, int c, double v) { dst.put(row ? rb : ra, c, v); });
+}
+
+// The middle of a solve in one kernel: for rows 2*blockIdx.x, +1 of x (m x m, the j-modes b, over
+// i), the DST along i, division by lam_r[b] + lam_c[a], and the DST back along a, written to dst.
+// The intermediate rows stay in shared memory (Y, 2m doubles after the tables).
+__global__ void __launch_bounds__(kFftThreads) k_dst_fft_divide(FftArgs F, const double* __restrict__ x,
+                                                                 const double* __restrict__ lam_r,
+                                                                 const double* __restrict__ lam_c, DstDest dst) {
+    extern __shared__ double2 fsm[];
+    double2* X = fsm;
+    double2* T = fsm + F.len;
+    double2* CS = fsm + 2 * F.len;
+    double* Y = reinterpret_cast<double*>(CS + F.ncs);  // the two rows between the transforms
+    const int m = F.m;
+    const int ra = 2 * blockIdx.x, rb = ra + 1;
+    const bool two = rb < m;
+    for (int t = threadIdx.x; t < F.ncs; t += kFftThreads) CS[t] = F.cs[t];
+    const double* xr[2] = {x + (size_t)ra * m, x + (size_t)rb * m};
+    const double lr[2] = {__ldg(lam_r + ra), two ? __ldg(lam_r + rb) : 1.0};
+    dst_row_pair(
+        F, X, T, CS, two, [&](int row, int c) { return __ldg(xr[row] + c); },
+        [&](int row, int c, double v) { Y[row * m + c] = v / (lr[row] + __ldg(lam_c + c)); });
+    dst_row_pair(
+        F, X, T, CS, two, [&](int row, int c) { return Y[row * m + c]; },
+        [&](int row, int c, double v) { dst.put(row ? rb : ra, c, v); });
 }
 
 // ------------------------------------------------------- dense fallback: out = X * S
@@ -320,11 +356,20 @@ cudaError_t transform_rows(const DstPlan& P, const double* x, int xld, int xo, d
 cudaError_t solve(const DstPlan& P, const double* in, double scale, const DstDest& d, cudaStream_t s) {
     const int m = P.m;
     const DstDest t1_tr{P.t1, m, 0, nullptr, nullptr, 0, 1, nullptr, nullptr};
-    const DstDest t2_div{P.t2, m, 0, nullptr, nullptr, 0, 0, P.lam_j, P.lam_i};  // rows b, columns a
     cudaError_t e;
     if ((e = transform_rows(P, in, P.n, 1, scale, t1_tr, s)) != cudaSuccess) return e;  // along j
-    if ((e = transform_rows(P, P.t1, m, 0, 1.0, t2_div, s)) != cudaSuccess) return e;   // along i, / lambda
-    if ((e = transform_rows(P, P.t2, m, 0, 1.0, t1_tr, s)) != cudaSuccess) return e;    // back along a
+    if (P.len) {
+        // along i, / lambda, back along a: one kernel, the rows staying in shared memory
+        const size_t smem = P.fft_smem + 2 * (size_t)m * sizeof(double);
+        k_dst_fft_divide<<<ceil_div(m, 2), kFftThreads, smem, s>>>(fft_args(P), P.t1, P.lam_j, P.lam_i,
+                                                                   DstDest{P.t2, m, 0, nullptr, nullptr, 0, 1,
+                                                                           nullptr, nullptr});
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        return transform_rows(P, P.t2, m, 0, 1.0, d, s);  // back along b
+    }
+    const DstDest t2_div{P.t2, m, 0, nullptr, nullptr, 0, 0, P.lam_j, P.lam_i};  // rows b, columns a
+    if ((e = transform_rows(P, P.t1, m, 0, 1.0, t2_div, s)) != cudaSuccess) return e;  // along i, / lambda
+    if ((e = transform_rows(P, P.t2, m, 0, 1.0, t1_tr, s)) != cudaSuccess) return e;   // back along a
     return transform_rows(P, P.t1, m, 0, 1.0, d, s);                                     // back along b
 }
 
@@ -371,7 +416,7 @@ int dst_plan_create(int n, double dx, double dy, DstPlan* P) {
         int ncs = 0;
         for (int s = 0; s < ns; ++s) ncs += radix[s];
         const size_t smem = (2 * (size_t)len + ncs) * sizeof(double2);
-        if (smem <= (size_t)smem_max) {
+        if (smem + 2 * (size_t)m * sizeof(double) <= (size_t)smem_max) {  // the fused middle pass's rows too
             P->len = len;
             P->nstages = ns;
             P->ncs = ncs;
@@ -401,7 +446,9 @@ int dst_plan_create(int n, double dx, double dy, DstPlan* P) {
                 cudaMemcpy(P->cs, cs.data(), ncs * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess ||
                 cudaMemcpy(P->sn, sn.data(), len * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
                 cudaFuncSetAttribute(k_dst_fft, cudaFuncAttributeMaxDynamicSharedMemorySize, P->fft_smem) !=
-                    cudaSuccess) {
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_dst_fft_divide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     P->fft_smem + 2 * m * (int)sizeof(double)) != cudaSuccess) {
                 dst_plan_destroy(P);
                 return CNV_CUDA_ERROR;
             }
