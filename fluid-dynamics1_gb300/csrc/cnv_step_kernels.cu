@@ -350,8 +350,11 @@ int post_grid(int n, int device) {
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_post, kStepThreads, 0) != cudaSuccess || per_sm < 1)
         return 0;
-    const int tiles = tile_count(n);
-    return tiles < sms * per_sm ? tiles : sms * per_sm;
+    // every block the same number of tiles: with more tiles than resident blocks, a grid of all
+    // resident blocks would leave some with one tile more than others in both phases
+    const int tiles = tile_count(n), resident = sms * per_sm;
+    const int per_block = (tiles + resident - 1) / resident;
+    return (tiles + per_block - 1) / per_block;
 }
 
 cudaError_t launch_post(const StepArgs& a, bool continuity, cudaStream_t s) {
