@@ -15,6 +15,8 @@
 //     2. along i, divided by lambda        (rows: b, over i-modes a)
 //     3. along a (inverse), written transposed (rows: i, over b)
 //     4. along b (inverse), into psi
+// On the FFT path passes 2 and 3 run as one kernel (k_dst_fft_divide): they transform the same
+// rows, so each block keeps its two rows in shared memory between them.
 // The eigenvalues are formed as sums of squared sines, not as den - 2 dy^2 cos - 2 dx^2 cos: that
 // difference cancels in the lowest modes (at n = 1024 it loses about four digits), while the
 // transforms themselves are orthogonal, so the solve is accurate to a few units of rounding
