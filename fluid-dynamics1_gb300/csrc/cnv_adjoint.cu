@@ -255,6 +255,7 @@ StepArgs base_args(const cnv_adjoint* a) {
     s.sor[1] = a->sor[1];
     s.ctrl = a->ctrl;
     s.timeout_ns = 2000000000LL;
+    s.tile_rows = step_tile_rows(a->n, a->device);
     return s;
 }
 

@@ -140,6 +140,7 @@ struct cnv_state {
     int cur = 0;                 // index of the current vorticity buffer
     int poisson_grid = 0, poisson_gx = 1, poisson_gy = 1;
     int cont_blocks = 0;
+    int tile_rows = 32;          // rows of the step passes' tiles
     PoissonParams pp{};
     StepArgs sa{};
 
@@ -509,7 +510,8 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
         s->poisson_grid = std::min(cfg->solver_blocks, std::min(std::min(per_sm, 2) * s->sms, kMaxSolverBlocks));
     poisson_tiles(n, s->poisson_grid, &s->poisson_gx, &s->poisson_gy);
     s->poisson_grid = s->poisson_gx * s->poisson_gy;
-    s->cont_blocks = post_grid(n, s->device);
+    s->tile_rows = step_tile_rows(n, s->device);
+    s->cont_blocks = post_grid(n, s->device, s->tile_rows);
     if (s->cont_blocks < 1) {
         free_state(s);
         return fail(CNV_CUDA_ERROR, "occupancy query failed for the post-solve pass");
@@ -662,6 +664,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     a.ctrl = s->ctrl;
     a.cont_partials = s->cont_partials;
     a.cont_blocks = s->cont_blocks;
+    a.tile_rows = s->tile_rows;
     a.timeout_ns = p.timeout_ns;
 
     if (cudaEventCreate(&s->ev0) != cudaSuccess || cudaEventCreate(&s->ev1) != cudaSuccess ||

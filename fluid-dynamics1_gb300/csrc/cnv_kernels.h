@@ -34,6 +34,7 @@ struct StepArgs {
     double* cont_partials;     // 4 * cont_blocks doubles
     int cont_blocks;           // blocks of the post pass's cooperative launch (post_grid)
     long long timeout_ns;      // bound on the post pass's grid barrier
+    int tile_rows;             // rows of the passes' 32-column tiles: 32, or 8 on small grids (step_tile_rows)
 };
 
 // Pre-solve pass: wall vorticity, derivatives, Euler update (w_in -> w_out, wall values into
@@ -42,8 +43,11 @@ cudaError_t launch_pre(const StepArgs& a, cudaStream_t s);
 // Post-solve pass: u, v and row-major psi from the split-layout psi in sor[]; with continuity,
 // also the continuity max/min and the step record (a cooperative launch of cont_blocks blocks).
 cudaError_t launch_post(const StepArgs& a, bool continuity, cudaStream_t s);
+// Rows of the passes' tiles for an n x n grid on `device`: 32, or 8 where 32-row tiles would give
+// fewer blocks than twice the SM count.
+int step_tile_rows(int n, int device);
 // Blocks of the post pass's cooperative launch for an n x n grid on `device` (0 on failure).
-int post_grid(int n, int device);
+int post_grid(int n, int device, int tile_rows);
 // Copy a row-major field into the split layout and back (parity tests of the solver alone).
 // to_split applies the same right-hand-side scaling as the transport pass (a.c4, a.rhs_mode).
 cudaError_t launch_to_split(const double* f, double* r, double* b, const StepArgs& a, cudaStream_t s);

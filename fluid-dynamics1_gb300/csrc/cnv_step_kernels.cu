@@ -58,12 +58,13 @@ constexpr int kPostVel = kMulInt;    // k_post: DY psi, DX psi
 constexpr int kPostCont = kMulInt;   // k_post: DX u, DY v
 
 constexpr int kTX = 32;                 // tile columns (one warp across)
-constexpr int kTY = 32;                 // tile rows
+// tile rows TY: 32 (each thread takes 4 cells of one column), or 8 on grids with fewer 32 x 32
+// tiles than twice the SM count (one cell per thread, four times the blocks: a 256^2 grid has
+// only 64 tiles of 32 x 32 for 152 SMs)
 constexpr int kR = 3;                   // stencil radius (order 6; orders 2 and 4 use less)
 constexpr int kSW = kTX + 2 * kR;       // staged row width
-constexpr int kSH = kTY + 2 * kR;       // staged rows
 constexpr int kStepThreads = 256;       // 32 x 8: each thread takes 4 cells of one column
-constexpr int kRowsPerThread = kTY / (kStepThreads / kTX);
+constexpr int kThreadRows = kStepThreads / kTX;  // 8 rows of threads
 constexpr int kBandDoubles = (int)(sizeof(FdBands) / sizeof(double));
 
 __device__ __forceinline__ double make_rhs(double f_ref, const StepArgs& a) {
@@ -98,12 +99,14 @@ __device__ __forceinline__ double wall_value(const StepArgs& a, const FdBands& b
 __device__ __forceinline__ bool on_edge(int i, int j, int n) { return i == 0 || i == n - 1 || j == 0 || j == n - 1; }
 
 // ----------------------------------------------------------------------------------- k_pre
+template <int TY>
 __global__ void __launch_bounds__(kStepThreads) k_pre(StepArgs a) {
+    constexpr int kSH = TY + 2 * kR;  // staged rows
     if (a.ctrl->abort) return;
     __shared__ double sw[kSH * kSW];
     __shared__ FdBands sb;
     const int n = a.n;
-    const int j0 = blockIdx.x * kTX, i0 = blockIdx.y * kTY;
+    const int j0 = blockIdx.x * kTX, i0 = blockIdx.y * TY;
     stage_bands(sb, a.bands);
     __syncthreads();
     // w on the tile and halo; edge cells take the wall value
@@ -122,8 +125,8 @@ __global__ void __launch_bounds__(kStepThreads) k_pre(StepArgs a) {
     auto W = [&](int r, int c) { return sw[(r - i0 + kR) * kSW + (c - j0 + kR)]; };
     const BoundaryValues bc = a.bc;
 #pragma unroll 1
-    for (int k = 0; k < kRowsPerThread; ++k) {
-        const int i = i0 + ty + k * (kStepThreads / kTX);
+    for (int k = 0; k < TY / kThreadRows; ++k) {
+        const int i = i0 + ty + k * kThreadRows;
         if (i >= n) break;
         const double wx = along_j<kPreD1>(sb.d1x, n, i, j, W);   // dwdx   = DX  w
         const double wy = along_i<kPreD1>(sb.d1y, n, i, j, W);   // dwdy   = DY  w
@@ -172,14 +175,16 @@ __device__ __forceinline__ void warp_ext(Ext& mx, Ext& mn) {
     }
 }
 
+template <int TY>
 __global__ void __launch_bounds__(kStepThreads) k_post(StepArgs a, int continuity) {
+    constexpr int kSH = TY + 2 * kR;  // staged rows
     if (a.ctrl->abort) return;  // stable for the whole launch: every block returns, or none
     __shared__ double sm[2 * kSH * kSW];  // phase 1: psi; phase 2: u and v
     __shared__ FdBands sb;
     __shared__ int s_ok;
     const int n = a.n;
     const int tiles_x = (n + kTX - 1) / kTX;
-    const int tiles = tiles_x * ((n + kTY - 1) / kTY);
+    const int tiles = tiles_x * ((n + TY - 1) / TY);
     const int tx = threadIdx.x % kTX, ty = threadIdx.x / kTX;
     stage_bands(sb, a.bands);
     __syncthreads();
@@ -189,7 +194,7 @@ __global__ void __launch_bounds__(kStepThreads) k_post(StepArgs a, int continuit
     const double* b = a.sor[1];
     const int pitch = a.pitch;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const int j0 = (tile % tiles_x) * kTX, i0 = (tile / tiles_x) * kTY;
+        const int j0 = (tile % tiles_x) * kTX, i0 = (tile / tiles_x) * TY;
         for (int x = threadIdx.x; x < kSH * kSW; x += kStepThreads) {
             const int rr = x / kSW, c = x - rr * kSW;
             const int i = i0 - kR + rr, j = j0 - kR + c;
@@ -200,8 +205,8 @@ __global__ void __launch_bounds__(kStepThreads) k_post(StepArgs a, int continuit
         const int j = j0 + tx;
         if (j < n) {
 #pragma unroll 1
-            for (int k = 0; k < kRowsPerThread; ++k) {
-                const int i = i0 + ty + k * (kStepThreads / kTX);
+            for (int k = 0; k < TY / kThreadRows; ++k) {
+                const int i = i0 + ty + k * kThreadRows;
                 if (i >= n) break;
                 const double uu = along_i<kPostVel>(sb.d1y, n, i, j, P);   // DY psi
                 const double vv = -along_j<kPostVel>(sb.d1x, n, i, j, P);  // -(DX psi)
@@ -230,7 +235,7 @@ __global__ void __launch_bounds__(kStepThreads) k_post(StepArgs a, int continuit
     double* su = sm;
     double* sv = sm + kSH * kSW;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const int j0 = (tile % tiles_x) * kTX, i0 = (tile / tiles_x) * kTY;
+        const int j0 = (tile % tiles_x) * kTX, i0 = (tile / tiles_x) * TY;
         for (int x = threadIdx.x; x < kSH * kSW; x += kStepThreads) {
             const int rr = x / kSW, c = x - rr * kSW;
             const int i = i0 - kR + rr, j = j0 - kR + c;
@@ -244,8 +249,8 @@ __global__ void __launch_bounds__(kStepThreads) k_post(StepArgs a, int continuit
         const int j = j0 + tx;
         if (j < n) {
 #pragma unroll 1
-            for (int k = 0; k < kRowsPerThread; ++k) {
-                const int i = i0 + ty + k * (kStepThreads / kTX);
+            for (int k = 0; k < TY / kThreadRows; ++k) {
+                const int i = i0 + ty + k * kThreadRows;
                 if (i >= n) break;
                 const double dudx = along_j<kPostCont>(sb.d1x, n, i, j, U);
                 const double dvdy = along_i<kPostCont>(sb.d1y, n, i, j, V);
@@ -336,31 +341,13 @@ __global__ void k_nonfinite(const double* x, long long count, int* flag) {
 
 dim3 grid2d(int n, dim3 blk) { return dim3((n + blk.x - 1) / blk.x, (n + blk.y - 1) / blk.y); }
 
-int tile_count(int n) { return ((n + kTX - 1) / kTX) * ((n + kTY - 1) / kTY); }
+int tile_count(int n, int ty) { return ((n + kTX - 1) / kTX) * ((n + ty - 1) / ty); }
 
-}  // namespace
-
-cudaError_t launch_pre(const StepArgs& a, cudaStream_t s) {
-    k_pre<<<dim3((a.n + kTX - 1) / kTX, (a.n + kTY - 1) / kTY), kStepThreads, 0, s>>>(a);
-    return cudaGetLastError();
-}
-
-int post_grid(int n, int device) {
-    int sms = 0, per_sm = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_post, kStepThreads, 0) != cudaSuccess || per_sm < 1)
-        return 0;
-    // every block the same number of tiles: with more tiles than resident blocks, a grid of all
-    // resident blocks would leave some with one tile more than others in both phases
-    const int tiles = tile_count(n), resident = sms * per_sm;
-    const int per_block = (tiles + resident - 1) / resident;
-    return (tiles + per_block - 1) / per_block;
-}
-
-cudaError_t launch_post(const StepArgs& a, bool continuity, cudaStream_t s) {
+template <int TY>
+cudaError_t launch_post_t(const StepArgs& a, bool continuity, cudaStream_t s) {
     int c = continuity ? 1 : 0;
     if (!continuity) {  // no barrier: one block per tile
-        k_post<<<tile_count(a.n), kStepThreads, 0, s>>>(a, c);
+        k_post<TY><<<tile_count(a.n, TY), kStepThreads, 0, s>>>(a, c);
         return cudaGetLastError();
     }
     // the grid barrier needs every block resident: a cooperative launch of at most post_grid blocks
@@ -376,7 +363,41 @@ cudaError_t launch_post(const StepArgs& a, bool continuity, cudaStream_t s) {
     cfg.numAttrs = 1;
     StepArgs args = a;
     void* kargs[] = {&args, &c};
-    return cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_post), kargs);
+    return cudaLaunchKernelExC(&cfg, reinterpret_cast<const void*>(&k_post<TY>), kargs);
+}
+
+}  // namespace
+
+int step_tile_rows(int n, int device) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms < 1) return 32;
+    return tile_count(n, 32) < 2 * sms ? 8 : 32;
+}
+
+cudaError_t launch_pre(const StepArgs& a, cudaStream_t s) {
+    if (a.tile_rows == 8)
+        k_pre<8><<<dim3((a.n + kTX - 1) / kTX, (a.n + 7) / 8), kStepThreads, 0, s>>>(a);
+    else
+        k_pre<32><<<dim3((a.n + kTX - 1) / kTX, (a.n + 31) / 32), kStepThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+int post_grid(int n, int device, int tile_rows) {
+    int sms = 0, per_sm = 0;
+    const void* kern =
+        tile_rows == 8 ? reinterpret_cast<const void*>(&k_post<8>) : reinterpret_cast<const void*>(&k_post<32>);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kStepThreads, 0) != cudaSuccess || per_sm < 1)
+        return 0;
+    // every block the same number of tiles: with more tiles than resident blocks, a grid of all
+    // resident blocks would leave some with one tile more than others in both phases
+    const int tiles = tile_count(n, tile_rows == 8 ? 8 : 32), resident = sms * per_sm;
+    const int per_block = (tiles + resident - 1) / resident;
+    return (tiles + per_block - 1) / per_block;
+}
+
+cudaError_t launch_post(const StepArgs& a, bool continuity, cudaStream_t s) {
+    return a.tile_rows == 8 ? launch_post_t<8>(a, continuity, s) : launch_post_t<32>(a, continuity, s);
 }
 
 cudaError_t launch_to_split(const double* f, double* r, double* b, const StepArgs& a, cudaStream_t s) {
