@@ -84,6 +84,7 @@ _SIGS = {
     "cnv_solver_info": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "cnv_probe_fp64": (C.c_int, [C.c_int, _dp, _dp]),
     "cnv_check_mul_rn": (C.c_int, [C.c_int, _dp, C.c_int, C.c_double, _dp]),
+    "cnv_check_div_rn": (C.c_int, [C.c_int, _dp, C.c_int, C.c_double, _dp, C.POINTER(C.c_longlong)]),
     "cnv_poisson_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int,
                                       C.c_int, C.c_double, C.c_int, C.c_double, C.POINTER(C.c_int), _dp,
                                       C.c_void_p]),
@@ -369,6 +370,16 @@ def check_mul_rn(x, c: float, device: int = 0):
     out = np.empty_like(x)
     check(load().cnv_check_mul_rn(device, _ptr(x), x.size, c, _ptr(out)), "cnv_check_mul_rn")
     return out
+
+
+def check_div_rn(x, b: float, device: int = 0):
+    """(x / b on the device the way the exact update divides by a constant, how many quotients
+    the three-operation path proved correctly rounded)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty_like(x)
+    fast = C.c_longlong(0)
+    check(load().cnv_check_div_rn(device, _ptr(x), x.size, b, _ptr(out), C.byref(fast)), "cnv_check_div_rn")
+    return out, fast.value
 
 
 def noise_field(n: int, seed: int, sigma: float = 1.0, passes: int = 0):

@@ -634,6 +634,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     p.den = 2 * (s->dx * s->dx + s->dy * s->dy);
     p.den_pow2 = is_pow2(p.den) ? 1 : 0;
     p.rden = 1.0 / p.den;
+    p.dden = div_const(p.den);
     p.wx = p.dx2 / p.den;
     p.wy = p.dy2 / p.den;
     p.b4 = p.beta / 4;
@@ -657,7 +658,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     a.c4 = s->dx * s->dx * s->dy * s->dy;
     // the mixed form takes g = c4*f as it is; the FP64 forms take their scaled variants
     a.rhs_mode = s->mixed ? 0 : (p.arith == Arith::kFma ? 1 : (p.fold ? 2 : 0));
-    a.rhs_den = p.den;
+    a.rhs_div = p.dden;
     a.rhs_rden = p.rden;
     a.rhs_den_pow2 = p.den_pow2;
     a.rhs_inv_h2 = 1.0 / p.dx2;

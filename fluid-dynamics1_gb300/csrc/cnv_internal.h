@@ -16,8 +16,10 @@
 //   ctrl          control block (barrier counter, status, abort flag, per-step records)
 #pragma once
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 
 #include "../../include/cnv.h"
 
@@ -70,6 +72,29 @@ struct Ctrl {
     int pad;
 };
 
+// Division by one constant b with the correctly rounded result (div_rn_const, cnv_sor.cuh):
+// the exact update's x / den when den is not a power of two. Built on the host by div_const.
+struct DivConst {
+    double b;                 // the divisor
+    double zh, zl;            // a two-term reciprocal: zh = RN(1/b), zl = RN(1/b - zh)
+    unsigned long long babs;  // bit pattern of |b|
+    int fast;                 // 1: 2^-100 <= |b| < 2^101, the range the fast path takes
+};
+
+// 1 - b*zh is a double (zh lies within half an ulp of 1/b), so one FMA gives it exactly and
+// zl = RN((1 - b*zh) / b) = RN(1/b - zh).
+inline DivConst div_const(double b) {
+    DivConst d{};
+    d.b = b;
+    d.zh = 1.0 / b;
+    d.zl = std::fma(-b, d.zh, 1.0) / b;
+    std::memcpy(&d.babs, &b, sizeof b);
+    d.babs &= 0x7fffffffffffffffull;
+    const int e = (int)(d.babs >> 52);
+    d.fast = e >= 1023 - 100 && e <= 1023 + 100 && std::isfinite(d.zl) ? 1 : 0;
+    return d;
+}
+
 // Arithmetic of the SOR point update.
 enum class Arith : int { kExact = 0, kFma = 1 };
 
@@ -85,6 +110,7 @@ struct PoissonParams {
     double den;         // 2*(dx*dx + dy*dy)
     double rden;        // 1/den when den is a power of two (then x/den == x*rden exactly)
     int den_pow2;
+    DivConst dden;      // x/den otherwise (div_const(den))
     double wx, wy;      // FMA form: dx2/den, dy2/den
     double b4;          // beta / 4 (exact), folded exact form
     int fold;           // 1: exact form with power-of-two scalings folded (dx = dy, dx^2 and den powers of 2)

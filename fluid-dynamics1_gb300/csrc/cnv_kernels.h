@@ -26,7 +26,7 @@ struct StepArgs {
     double c4;                 // dx*dx*dy*dy (src/poisson.c:247 evaluates it left to right)
     int rhs_mode;              // 0: rhs = c4*f; 1: rhs = (c4*f) / den (FMA form);
                                // 2: rhs = (c4*f) * (1/dx^2), an exact power-of-two scaling (folded form)
-    double rhs_den;
+    DivConst rhs_div;          // division by den (rhs_mode 1, den not a power of two)
     double rhs_rden;
     int rhs_den_pow2;
     double rhs_inv_h2;

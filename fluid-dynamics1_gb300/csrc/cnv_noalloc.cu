@@ -124,6 +124,7 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
     int e2 = 0;
     p.den_pow2 = std::frexp(p.den, &e2) == 0.5 ? 1 : 0;
     p.rden = 1.0 / p.den;
+    p.dden = div_const(p.den);
     p.wx = p.dx2 / p.den;
     p.wy = p.dy2 / p.den;
     p.b4 = p.beta / 4;
@@ -135,7 +136,7 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
     a.pitch = pitch;
     a.c4 = dx * dx * dy * dy;
     a.rhs_mode = p.arith == Arith::kFma ? 1 : (p.fold ? 2 : 0);
-    a.rhs_den = p.den;
+    a.rhs_div = p.dden;
     a.rhs_rden = p.rden;
     a.rhs_den_pow2 = p.den_pow2;
     a.rhs_inv_h2 = 1.0 / p.dx2;

@@ -37,7 +37,7 @@
 //
 // Arithmetic. Arith::kExact reproduces the reference's point update bit for bit: in general with
 // the full operation sequence of src/poisson.c:247 (division by 2*(dx^2+dy^2) exact when that is
-// a power of two, IEEE division otherwise); when dx = dy and dx^2 and 2*(dx^2+dy^2) are powers of
+// a power of two, otherwise the correctly rounded division by a constant of cnv_sor.cuh); when dx = dy and dx^2 and 2*(dx^2+dy^2) are powers of
 // two (every n = 2^k with L = 1), with the folded form
 //     new = RN(RN(beta/4 * RN(RN(RN(up+dn) + RN(rt+lt)) - g')) + RN((1-beta)*old))
 // with g' = c4*f / dx^2, which equals the reference's value whenever no intermediate

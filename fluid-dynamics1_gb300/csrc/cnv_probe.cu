@@ -69,6 +69,16 @@ __global__ void k_mul_rn(const double* x, int count, double c, double* out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) out[i] = mul_rn(c, x[i]);
 }
 
+__global__ void k_div_rn(const double* x, int count, DivConst d, double* out, unsigned long long* fast) {
+    unsigned long long mine = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        double q;
+        if (div_rn_const_fast(x[i], d, q)) ++mine;
+        out[i] = div_rn_const(x[i], d);
+    }
+    if (mine) atomicAdd(fast, mine);
+}
+
 }  // namespace
 }  // namespace cnv
 
@@ -94,6 +104,37 @@ extern "C" int cnv_check_mul_rn(int device, const double* x, int count, double c
     }
     cudaFree(d);
     if (rc != CNV_OK) set_last_error("cnv_check_mul_rn: kernel or copy failed");
+    return rc;
+}
+
+extern "C" int cnv_check_div_rn(int device, const double* x, int count, double b, double* out, long long* fast) {
+    using namespace cnv;
+    if (!x || !out || count < 0) {
+        set_last_error("cnv_check_div_rn: bad argument");
+        return CNV_BAD_ARG;
+    }
+    if (fast) *fast = 0;
+    if (count == 0) return CNV_OK;
+    double* d = nullptr;
+    const size_t bytes = (size_t)count * sizeof(double);
+    int rc = CNV_OK;
+    if (cudaSetDevice(device) != cudaSuccess || cudaMalloc(&d, 2 * bytes + sizeof(unsigned long long)) != cudaSuccess) {
+        set_last_error("cnv_check_div_rn: device setup failed");
+        return CNV_CUDA_ERROR;
+    }
+    unsigned long long* nf = reinterpret_cast<unsigned long long*>(d + 2 * (size_t)count);
+    if (cudaMemcpy(d, x, bytes, cudaMemcpyHostToDevice) != cudaSuccess || cudaMemset(nf, 0, sizeof *nf) != cudaSuccess)
+        rc = CNV_CUDA_ERROR;
+    if (rc == CNV_OK) {
+        k_div_rn<<<(count + 255) / 256 < 4096 ? (count + 255) / 256 : 4096, 256>>>(d, count, div_const(b), d + count, nf);
+        unsigned long long h = 0;
+        if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, d + count, bytes, cudaMemcpyDeviceToHost) != cudaSuccess ||
+            cudaMemcpy(&h, nf, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess)
+            rc = CNV_CUDA_ERROR;
+        if (fast) *fast = (long long)h;
+    }
+    cudaFree(d);
+    if (rc != CNV_OK) set_last_error("cnv_check_div_rn: kernel or copy failed");
     return rc;
 }
 

@@ -192,8 +192,9 @@ __device__ __forceinline__ bool big_or_zero(double x) {
 // IEEE 754 round-half-to-even rule on the rest. A zero x gives the signed zero. Returns false
 // (the caller multiplies on the FP64 pipe instead) for a subnormal, infinite or NaN x, a c that
 // is not normal, and products outside the normal range, so every result equals __dmul_rn(x, c).
-// The exact update uses it for its two multiplications by constants, which moves them from the
-// FP64 pipe (the solver's bottleneck at 7 FP64 operations per cell) to the integer pipes.
+// The exact update uses it for its multiplications by constants (two in the folded form, four in
+// the general one), which moves them from the FP64 pipe (the solver's bottleneck) to the integer
+// pipes.
 __device__ __forceinline__ bool mul_rn_int(double x, unsigned long long cb, double& out) {
     const unsigned long long xb = (unsigned long long)__double_as_longlong(x);
     const unsigned long long sign = (xb ^ cb) & 0x8000000000000000ull;
@@ -242,6 +243,42 @@ __device__ __forceinline__ double mul_rn(double c, double x) {
     return r;
 }
 
+// The quotient a / d.b from the two-term reciprocal, q = RN(a*zh + RN(a*zl)) (the method of
+// Brisebarre, Muller and Raina, "Accelerating correctly rounded floating-point division when the
+// divisor is known in advance", IEEE Trans. Computers 53(8), 2004), with an exact test that q is
+// a / b rounded to nearest. Returns false (q unproven) outside the tested range, for a q that is
+// a power of two, and where the test fails.
+// The test. If |q - a/b| < ulp(q), the residual a - b*q is a double (it is a multiple of
+// ulp(b)*ulp(q) below |b|*ulp(q) in magnitude), so one FMA gives it exactly; q = RN(a/b) iff
+// |a/b - q| < ulp(q)/2, i.e. |r| < |b| * ulp(q)/2, for q not a power of two (whose lower
+// neighbour is nearer); equality (a tie) is left to the caller. If |q - a/b| >= ulp(q),
+// |a - b*q| >= |b| * ulp(q), which no rounding brings below the bound, so the test fails. With
+// 2^-700 <= |a| < 2^701 and 2^-100 <= |b| < 2^101 (d.fast) every value here stays normal.
+// q is within ulp(q)/2 + 2^-104 |a/b| of a/b, so the test fails only for quotients that close to
+// a tie: the division costs three FP64 operations and a few integer ones.
+__device__ __forceinline__ bool div_rn_const_fast(double a, const DivConst& d, double& out) {
+    const unsigned long long ab = (unsigned long long)__double_as_longlong(a);
+    const int ea = (int)((ab >> 52) & 0x7ff);
+    if (!d.fast || ea < 1023 - 700 || ea > 1023 + 700) return false;
+    const double q = __fma_rn(a, d.zh, __dmul_rn(a, d.zl));
+    const double r = __fma_rn(-q, d.b, a);  // a - b*q
+    const unsigned long long qb = (unsigned long long)__double_as_longlong(q);
+    const unsigned long long rb = (unsigned long long)__double_as_longlong(r) & 0x7fffffffffffffffull;
+    const int eq = (int)((qb >> 52) & 0x7ff);
+    // |b| * ulp(q) / 2 = |b| * 2^(eq - 1023 - 53): an exponent shift of |b|'s bit pattern
+    const unsigned long long hb = d.babs + ((unsigned long long)(long long)(eq - 1076) << 52);
+    if ((qb & ((1ull << 52) - 1)) == 0 || rb >= hb) return false;
+    out = q;
+    return true;
+}
+
+// a / d.b rounded to nearest, ties to even: the same bits as __ddiv_rn(a, d.b).
+__device__ __forceinline__ double div_rn_const(double a, const DivConst& d) {
+    double q;
+    if (!div_rn_const_fast(a, d, q)) q = __ddiv_rn(a, d.b);
+    return q;
+}
+
 // The new value of one cell (no norm).
 template <Arith A, int KIND, bool FOLD>
 __device__ __forceinline__ double point_value(const PoissonParams& p, double up, double dn, double rt,
@@ -268,15 +305,18 @@ __device__ __forceinline__ double point_value(const PoissonParams& p, double up,
                     nw = __dmul_rn(num, p.rden);
             }
         } else {
-            // beta*(dy*dy*(up+dn) + dx*dx*(rt+lt) - dx*dx*dy*dy*f) / (2*(dx*dx+dy*dy)) + (1-beta)*u0
-            const double num = __dsub_rn(__dadd_rn(__dmul_rn(p.dy2, __dadd_rn(up, dn)),
-                                                   __dmul_rn(p.dx2, __dadd_rn(rt, lt))), g);
+            // beta*(dy*dy*(up+dn) + dx*dx*(rt+lt) - dx*dx*dy*dy*f) / (2*(dx*dx+dy*dy)) + (1-beta)*u0,
+            // its four multiplications by constants on the integer pipes and the division by den
+            // as three FP64 operations (div_rn_const): 8 on the FP64 pipe where the IEEE division
+            // alone took more (1536^2: 88.6 -> 60.6 us per sweep, the same bits)
+            const double num = __dsub_rn(__dadd_rn(mul_rn(p.dy2, __dadd_rn(up, dn)),
+                                                   mul_rn(p.dx2, __dadd_rn(rt, lt))), g);
             if (KIND == CNV_POISSON_SOR) {
-                const double bn = __dmul_rn(p.beta, num);
-                const double q = p.den_pow2 ? __dmul_rn(bn, p.rden) : __ddiv_rn(bn, p.den);
-                nw = __dadd_rn(q, __dmul_rn(p.omb, old));
+                const double bn = mul_rn(p.beta, num);
+                const double q = p.den_pow2 ? __dmul_rn(bn, p.rden) : div_rn_const(bn, p.dden);
+                nw = __dadd_rn(q, mul_rn(p.omb, old));
             } else {
-                nw = p.den_pow2 ? __dmul_rn(num, p.rden) : __ddiv_rn(num, p.den);
+                nw = p.den_pow2 ? __dmul_rn(num, p.rden) : div_rn_const(num, p.dden);
             }
         }
         return nw;

@@ -70,7 +70,7 @@ constexpr int kBandDoubles = (int)(sizeof(FdBands) / sizeof(double));
 __device__ __forceinline__ double make_rhs(double f_ref, const StepArgs& a) {
     // src/poisson.c:247 multiplies dx*dx*dy*dy*f left to right: (((dx*dx)*dy)*dy)*f = c4*f
     double g = dmul(a.c4, f_ref);
-    if (a.rhs_mode == 1) g = a.rhs_den_pow2 ? dmul(g, a.rhs_rden) : __ddiv_rn(g, a.rhs_den);
+    if (a.rhs_mode == 1) g = a.rhs_den_pow2 ? dmul(g, a.rhs_rden) : div_rn_const(g, a.rhs_div);
     else if (a.rhs_mode == 2) g = dmul(g, a.rhs_inv_h2);  // exact: 1/dx^2 is a power of two
     return g;
 }

@@ -346,6 +346,11 @@ int cnv_probe_fp64(int device, double *add_mul_ops_per_s, double *fma_ops_per_s)
  * constants (integer arithmetic where it applies, the FP64 pipe otherwise): every result must
  * equal the correctly rounded IEEE product. Host arrays of count doubles. */
 int cnv_check_mul_rn(int device, const double *x, int count, double c, double *out);
+/* out[i] = x[i] / b computed on the device exactly as the exact Poisson update and the transport
+ * pass divide by a constant that is not a power of two: every result must equal the correctly
+ * rounded IEEE quotient. *fast (may be NULL) receives how many quotients the three-operation
+ * path proved correctly rounded (the rest took the IEEE division). Host arrays of count doubles. */
+int cnv_check_div_rn(int device, const double *x, int count, double b, double *out, long long *fast);
 
 /* Human-readable text for the last failing call on this thread. */
 const char *cnv_last_error(void);

@@ -70,3 +70,83 @@ def test_halfway_products_round_to_even(cnv):
             with np.errstate(all="ignore"):
                 want = x * c
             assert same_bits(got, want).all(), (expo, c)
+
+
+# ---------------------------------------------------------------------------------------------
+# Division by a constant (csrc/cnv_sor.cuh, div_rn_const): the exact update's x / den and the
+# transport pass's (c4 f) / den on grids where den = 2 (dx^2 + dy^2) is not a power of two (every
+# n that is not a power of two, dx = L / n as src/main.c:138 sets it). The quotient comes from a
+# two-term reciprocal and an exact residual test, with the IEEE division where the test cannot
+# prove it; every result must equal numpy's correctly rounded quotient.
+
+def den_of(n, L=1.0):
+    dx = L / n
+    return 2 * (dx * dx + dx * dx)
+
+
+DIVISORS = [den_of(768), den_of(1536), den_of(100), den_of(37), den_of(7), den_of(3000), 3.0, -7.0, 0.1,
+            1.0 / 3.0, 1 + 2.0 ** -52, 2 - 2.0 ** -52, -(2 - 2.0 ** -52), 0.75, 2.0 ** -30,
+            2.0 ** -100 * 1.5, 2.0 ** 100 * 1.999, 2.0 ** 101 * 1.25, 2.0 ** -101 * 1.75, 1e-300, 1e300]
+
+
+def _significand(b):
+    m, e = math.frexp(abs(b))  # abs(b) = m * 2^e, 0.5 <= m < 1
+    B = int(m * 2 ** 53)
+    return B, e - 53
+
+
+def near_ties(b, count, seed):
+    """Dividends a with a / b within about 2^-105 (relative) of a tie between two doubles: with
+    b = B * 2^eb (B odd), pick an odd 54-bit M with B*M = t (mod 2^k) for a small odd t, so that
+    A = (B*M - t) / 2^k is a 53-bit integer and a = A * 2^E gives a / b = (M - t/B) * 2^x, where
+    M * 2^x is the midpoint between two consecutive doubles."""
+    rng = np.random.default_rng(seed)
+    B, eb = _significand(b)
+    while B % 2 == 0:
+        B //= 2
+        eb += 1
+    nb = B.bit_length()
+    out = []
+    while len(out) < count:
+        t = int(rng.integers(-7, 8)) * 2 + 1
+        k = nb + int(rng.integers(0, 2))
+        M0 = (t * pow(B, -1, 1 << k)) % (1 << k)
+        lo = -(-((1 << 53) - M0) // (1 << k))
+        hi = ((1 << 54) - 1 - M0) // (1 << k)
+        if lo > hi:
+            continue
+        M = M0 + int(rng.integers(lo, hi + 1)) * (1 << k)
+        P = B * M - t
+        A = P >> k
+        if P % (1 << k) or not (1 << 52) <= A < (1 << 53):
+            continue
+        a = math.ldexp(A, int(rng.integers(-60, 60)))
+        out.append(-a if rng.integers(0, 2) else a)
+    return np.array(out)
+
+
+@pytest.mark.parametrize("b", DIVISORS)
+def test_division_by_constant_is_correctly_rounded(cnv, b):
+    rng = np.random.default_rng(abs(hash(b)) % (1 << 32))
+    x = np.concatenate([operands(rng, 1 << 20), near_ties(b, 4000, 1)])
+    got, fast = cnv.check_div_rn(x, b)
+    with np.errstate(all="ignore"):
+        want = x / b
+    bad = ~same_bits(got, want)
+    assert not bad.any(), f"b={b!r}: {bad.sum()} mismatches, first x={x[bad][0]!r}: {got[bad][0]!r} vs {want[bad][0]!r}"
+    assert 0 <= fast <= x.size
+
+
+@pytest.mark.parametrize("n", [768, 1536, 100, 37])
+def test_division_by_den_takes_the_short_path(cnv, n):
+    """On dividends of the solver's range (|x| between 2^-60 and 2^20) the three-operation path
+    proves nearly every quotient; only the constructed near-ties may need the IEEE division."""
+    b = den_of(n)
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(1 << 20) * np.exp2(rng.integers(-60, 20, size=1 << 20))
+    got, fast = cnv.check_div_rn(x, b)
+    assert same_bits(got, x / b).all()
+    assert fast >= 0.999 * x.size, fast / x.size
+    ties = near_ties(b, 2000, n)
+    got, _ = cnv.check_div_rn(ties, b)
+    assert same_bits(got, ties / b).all()
