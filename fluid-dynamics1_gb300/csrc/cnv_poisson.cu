@@ -623,14 +623,15 @@ void poisson_tiles(int n, int grid, int* gx, int* gy) {
 }
 
 int poisson_grid_for(int n, int sms, int per_sm) {
-    // Two blocks per SM from about 3000 interior cells per block: the second block's warps hide
-    // FP64 latency (1024^2: 18.0 us per sweep on 2 x 152 blocks, 18.8 on 152); one per SM from
-    // about 700 cells per block (768^2: 26.0 us on 152 blocks, 26.9 on 304); below that one
+    // Two blocks per SM from about 1800 interior cells per block: the second block's warps hide
+    // FP64 latency (1024^2: 18.0 us per sweep on 2 x 152 blocks, 18.8 on 152; 768^2: 21.2 on
+    // 304, 23.0 on 152; 640^2: 17.0 on 304, 16.6 on 152); one per SM from
+    // about 700 cells per block; below that one
     // block per about 700 cells, picking among the nearby counts the one whose tiles have the
     // smallest frames (a prime count would only tile as strips).
     const long long cells = (long long)(n - 2) * (n - 2);
     const int cap = std::min(std::min(per_sm, 2) * sms, kMaxSolverBlocks);
-    if (cells >= 2LL * sms * 3000 && cap >= 2 * sms) return 2 * sms;
+    if (cells >= 2LL * sms * 1800 && cap >= 2 * sms) return 2 * sms;
     if (cells >= 700LL * sms) return std::min(sms, cap);
     const int want = (int)std::max(1LL, std::min<long long>(cells / 700, cap));
     const double ni = n - 2;
