@@ -50,7 +50,10 @@ int fail(int status, const char* fmt, ...) {
 // Sweeps per border exchange the FP64 SOR/GS solve uses by default for an n x n grid (1: the
 // kernel that exchanges every half-sweep; measured per sweep: 256^2 6.7 us tiled vs 8.6, 320^2
 // 12.3 vs 11.3, 512^2 11.4 vs 9.1, 768^2 31.5 vs 26.0).
-int auto_sor_sweeps(int n) { return n < 300 ? 4 : 1; }
+// Sweeps per border exchange by grid size, from timings of both kernels on the cavity workload
+// (us per sweep, exchange kernel vs 2 / 4 sweeps per exchange): 256^2 7.38 vs 6.57 / 6.17,
+// 288^2 9.30 vs 8.90 / 8.85, 320^2 9.70 vs 9.42 / 10.12, 352^2 9.67 vs 10.11 / 10.99.
+int auto_sor_sweeps(int n) { return n < 300 ? 4 : n < 336 ? 2 : 1; }
 
 bool is_pow2(double x) {
     int e;
@@ -507,7 +510,7 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     }
     s->poisson_grid = poisson_grid_for(n, s->sms, per_sm);
     if (cfg->solver_blocks > 0)
-        s->poisson_grid = std::min(cfg->solver_blocks, std::min(std::min(per_sm, 2) * s->sms, kMaxSolverBlocks));
+        s->poisson_grid = std::min(cfg->solver_blocks, std::min(per_sm * s->sms, kMaxSolverBlocks));
     poisson_tiles(n, s->poisson_grid, &s->poisson_gx, &s->poisson_gy);
     s->poisson_grid = s->poisson_gx * s->poisson_gy;
     s->tile_rows = step_tile_rows(n, s->device);

@@ -8,18 +8,18 @@
 // (src/poisson.c:34-60, :272-278); the iterate of that sweep is the answer and k is reported.
 //
 // Decomposition. The interior is cut into GX x GY tiles, one block per tile and at most one
-// block per SM (or two), so every SM gets the same work. psi is kept in two copies ("sets") of
+// block per SM, so every SM gets the same work. psi is kept in two copies ("sets") of
 // the red/black split layout: sweep k reads set (k-1)&1 and writes set k&1, so the state of
 // sweep k stays intact while sweep k+1 runs. A tile's interior cells depend only on the tile's
 // own data; its frame (first/last row/column next to another tile) reads the neighbours'.
 //
-// Warp roles. Fifteen warps update cells; the sixteenth (the signal warp) does all inter-block
+// Warp roles. Thirty-one warps update cells; the last (the signal warp) does all inter-block
 // work: it polls the four neighbours' progress flags, raises this block's flag once the frame
 // is written (fence + release store), adds the block's share of the stop norm to the global
 // accumulator and runs the stop test. The two sides meet only at named barriers that the
 // cell-update warps pass through without waiting for any fence or poll (bar.arrive where they
 // hand something over, bar.sync only where they need the signal warp's answer, which it
-// prepares ahead). In each half-sweep the first four warps wait for the neighbours' frames
+// prepares ahead). In each half-sweep the first twelve warps wait for the neighbours' frames
 // (barrier GO), update this colour's frame and hand it to the signal warp (PUB); every
 // cell-update warp then takes 32-cell chunks of the interior from a shared counter, so the
 // frame's latency is covered by the other warps' interior work and the FP64 pipe never idles
@@ -54,12 +54,19 @@
 namespace cnv {
 namespace {
 
-constexpr int kThreads = 512;
+// One block of 1024 threads per SM. Against two blocks of 512 (15 cell warps and 4 frame warps
+// each) it gave the same bits and 10.19 vs 12.14 us per sweep at 384^2, 8.66 vs 9.96 at 512^2,
+// 20.50 vs 21.16 at 768^2, 17.08 vs 17.14 at 1024^2, 61.16 vs 60.63 at 1536^2 and 53.95 vs 56.24
+// at 2048^2: no block shares its SM's FP64 pipe with another block's (in the two-block layout
+// the second block on each SM ran its sweeps about 0.5 us slower, and the slowest blocks pace
+// the grid), and the larger tiles have half the frame per cell. Eight frame warps gave 17.12 and
+// 54.21, four 18.18 and 54.20 us at 1024^2 and 2048^2.
+constexpr int kThreads = 1024;
 constexpr int kWarps = kThreads / 32;
-constexpr int kCellWarps = kWarps - 1;          // warps 0..14 update cells
+constexpr int kCellWarps = kWarps - 1;          // warps 0..30 update cells
 constexpr int kCellThreads = kCellWarps * 32;
-constexpr int kSignalWarp = kWarps - 1;         // warp 15: flags, norm, stop test
-constexpr int kFrameWarps = 4;                  // warps 0..3 also update the frame
+constexpr int kSignalWarp = kWarps - 1;         // warp 31: flags, norm, stop test
+constexpr int kFrameWarps = 12;                 // warps 0..11 also update the frame
 constexpr int kFrameThreads = kFrameWarps * 32;
 constexpr int kRing = 8;
 
@@ -514,7 +521,7 @@ __device__ void cell_warps(const PoissonLaunch& L, const Tile& t, Shared& sh) {
 }
 
 template <Arith A, int KIND, bool FOLD>
-__global__ void __launch_bounds__(kThreads, 2) k_poisson(PoissonLaunch L) {
+__global__ void __launch_bounds__(kThreads, 1) k_poisson(PoissonLaunch L) {
     Ctrl* ctl = L.ctrl;
     const PoissonParams& p = L.p;
     SyncState* sy = reinterpret_cast<SyncState*>(L.sync);
@@ -623,15 +630,11 @@ void poisson_tiles(int n, int grid, int* gx, int* gy) {
 }
 
 int poisson_grid_for(int n, int sms, int per_sm) {
-    // Two blocks per SM from about 1800 interior cells per block: the second block's warps hide
-    // FP64 latency (1024^2: 18.0 us per sweep on 2 x 152 blocks, 18.8 on 152; 768^2: 21.2 on
-    // 304, 23.0 on 152; 640^2: 17.0 on 304, 16.6 on 152); one per SM from
-    // about 700 cells per block; below that one
-    // block per about 700 cells, picking among the nearby counts the one whose tiles have the
-    // smallest frames (a prime count would only tile as strips).
+    // One block per SM from about 700 interior cells per block; below that one block per about
+    // 700 cells, picking among the nearby counts the one whose tiles have the smallest frames (a
+    // prime count would only tile as strips).
     const long long cells = (long long)(n - 2) * (n - 2);
-    const int cap = std::min(std::min(per_sm, 2) * sms, kMaxSolverBlocks);
-    if (cells >= 2LL * sms * 1800 && cap >= 2 * sms) return 2 * sms;
+    const int cap = std::min(std::min(per_sm, 1) * sms, kMaxSolverBlocks);
     if (cells >= 700LL * sms) return std::min(sms, cap);
     const int want = (int)std::max(1LL, std::min<long long>(cells / 700, cap));
     const double ni = n - 2;

@@ -302,7 +302,7 @@ int cnv_last_stats(cnv_state *s, long long *sweeps, double *ms, double *poisson_
 int cnv_time_passes(cnv_state *s, int reps, double *pre_ms, double *post_ms);
 
 /* One line naming the Poisson solver this state runs and its geometry, e.g.
- * "sor-exchange grid=304 tiles=16x19" (FP64 SOR/GS exchanging every half-sweep),
+ * "sor-exchange grid=152 tiles=8x19" (FP64 SOR/GS exchanging every half-sweep),
  * "sor-tiled sweeps=4 grid=150 tiles=5x30", "mixed grid=152 tiles=8x19" or
  * "direct-sine-transform". Returns CNV_BAD_ARG if it does not fit in len bytes. */
 int cnv_solver_info(cnv_state *s, char *buf, size_t len);

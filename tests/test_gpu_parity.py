@@ -321,18 +321,18 @@ def test_blocking_flag_checks(cnv):
 
 @pytest.mark.parametrize("n,kw,want", [
     (256, {}, "sor-tiled sweeps=4"),                       # the tiled kernel below 300^2
-    (320, {}, "sor-exchange"),                             # the exchange kernel from 300^2
+    (320, {}, "sor-tiled sweeps=2"),                       # two sweeps per exchange from 300^2
+    (352, {}, "sor-exchange"),                             # the exchange kernel from 336^2
     (512, {}, "sor-exchange grid=152 tiles=8x19"),         # one block per SM (not 127 strips)
-    (1024, {}, "sor-exchange grid=304 tiles=16x19"),       # two blocks per SM
-    (768, {}, "sor-exchange grid=304"),                    # two from about 3600 cells per SM
-    (640, {}, "sor-exchange grid=152"),
+    (1024, {}, "sor-exchange grid=152 tiles=8x19"),        # one block of 1024 threads per SM
+    (2048, {}, "sor-exchange grid=152 tiles=8x19"),
     (1024, {"precision": 2}, "mixed grid=152"),
     (256, {"poisson_type": 4}, "direct-sine-transform"),
     (256, {"sor_blocking": 1}, "sor-exchange"),
 ])
 def test_solver_choice_and_geometry(cnv, n, kw, want):
     """cnv_solver_info names the solver a state picked; the defaults follow the measured
-    crossovers (tiled kernel below 300^2, one block per SM up to about 3600 cells per SM)."""
+    crossovers (tiled kernel below 336^2, then one block per SM)."""
     with cnv.Cavity(make_cfg(cnv, n, **kw)) as cav:
         info = cav.solver_info()
     assert info.startswith(want), info
