@@ -641,6 +641,8 @@ int cnv_create(const cnv_config* cfg, cnv_state** out) {
     p.wx = p.dx2 / p.den;
     p.wy = p.dy2 / p.den;
     p.b4 = p.beta / 4;
+    p.kb4 = mul_const(p.b4);
+    p.komb = mul_const(p.omb);
     p.timeout_ns = (cfg->solver_timeout_ms > 0 ? cfg->solver_timeout_ms : 2000) * 1000000LL;  // per wait
     p.stall_block = cfg->test_stall_block - 1;
 

@@ -95,6 +95,28 @@ inline DivConst div_const(double b) {
     return d;
 }
 
+// A constant of the exact update's integer multiply (mul_rn_k, cnv_sor.cuh), prepared on the host
+// so that the kernel reads its significand, exponent and sign from the launch parameters.
+struct MulConst {
+    double c;
+    unsigned long long m;     // significand with its leading bit, 2^52 <= m < 2^53
+    unsigned long long sign;  // sign bit of c, in place
+    int e;                    // biased exponent of c
+    int ok;                   // c is a normal number (else the FP64 multiply is used)
+};
+
+inline MulConst mul_const(double c) {
+    MulConst k{};
+    k.c = c;
+    unsigned long long b;
+    std::memcpy(&b, &c, sizeof b);
+    k.sign = b & 0x8000000000000000ull;
+    k.e = (int)((b >> 52) & 0x7ff);
+    k.m = (b & ((1ull << 52) - 1)) | (1ull << 52);
+    k.ok = k.e != 0 && k.e != 0x7ff ? 1 : 0;
+    return k;
+}
+
 // Arithmetic of the SOR point update.
 enum class Arith : int { kExact = 0, kFma = 1 };
 
@@ -113,6 +135,7 @@ struct PoissonParams {
     DivConst dden;      // x/den otherwise (div_const(den))
     double wx, wy;      // FMA form: dx2/den, dy2/den
     double b4;          // beta / 4 (exact), folded exact form
+    MulConst kb4, komb;  // b4 and omb for the folded form's integer multiply
     int fold;           // 1: exact form with power-of-two scalings folded (dx = dy, dx^2 and den powers of 2)
     long long timeout_ns;  // bound on every wait for another block
     int stall_block;       // testing only: block of the exchange kernel that never raises its flags (-1: none)

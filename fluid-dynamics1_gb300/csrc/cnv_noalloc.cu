@@ -128,6 +128,8 @@ extern "C" int cnv_poisson_noalloc(const double* f, double* psi, int n, double d
     p.wx = p.dx2 / p.den;
     p.wy = p.dy2 / p.den;
     p.b4 = p.beta / 4;
+    p.kb4 = mul_const(p.b4);
+    p.komb = mul_const(p.omb);
     p.timeout_ns = 2000000000LL;
     p.stall_block = -1;
 

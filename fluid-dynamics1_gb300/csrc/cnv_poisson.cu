@@ -226,6 +226,56 @@ __device__ __forceinline__ void interior_chunks(const PoissonParams& p, const Ti
     const double* __restrict__ O = q.oth[C];
     const double* __restrict__ G = q.rhs[C];
     const int pitch = p.pitch;
+    if (FOLD && wq >= 48) {
+        // Row-aligned chunks: chunk c is cells [64 b, 64 b + 64) of row r (b = c % per_row) of
+        // this colour, so the row, its parity and the neighbour offsets are the same for the whole
+        // chunk and a cell's address is the row's base plus its index (no division per cell).
+        // Taken where a row holds at least 48 cells of a colour, so that few lanes idle (1024^2:
+        // 16.73 vs 16.84 us per sweep, 2048^2: 52.5 vs 53.2, the same bits); the general form keeps
+        // the flat chunks, with which its kernel ran faster.
+        const int per_row = (wq + 63) >> 6;
+        const unsigned nrc = (unsigned)(h * per_row);
+        for (;;) {
+            unsigned c = 0;
+            if (lane == 0) c = atomicAdd(ctr, 1u);
+            c = __shfl_sync(0xffffffffu, c, 0);
+            if (c >= nrc) break;
+            const int r = (int)c / per_row;
+            const int b = (int)c - r * per_row;
+            const int i = t.ri0 + r;
+            const int j0 = t.ci0 + ((i + t.ci0 + C) & 1);  // the row's first cell of colour C
+            const int jl = ((j0 - 1) >> 1) - (j0 >> 1);     // -1 or 0: the left neighbour's offset
+            const int jr = ((j0 + 1) >> 1) - (j0 >> 1);     // 0 or +1
+            const size_t base = (size_t)i * pitch + (j0 >> 1);
+            size_t at[2];
+            bool ok[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const int tt = b * 64 + u * 32 + lane;  // cell j0 + 2 tt of the row
+                ok[u] = tt < wq && j0 + 2 * tt < t.ci1;
+                at[u] = base + (ok[u] ? tt : 0);
+            }
+            double old[2], up[2], dn[2], lt[2], rt[2], g[2];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                old[u] = Sp[at[u]];
+                up[u] = O[at[u] + pitch];
+                dn[u] = O[at[u] - pitch];
+                lt[u] = O[at[u] + jl];
+                rt[u] = O[at[u] + jr];
+                g[u] = __ldg(G + at[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const double nw = point_value<A, KIND, FOLD>(p, up[u], dn[u], rt[u], lt[u], g[u], old[u]);
+                if (ok[u]) {
+                    Sn[at[u]] = nw;
+                    if (!norm_add(acc, nw, old[u])) norm_side_add(side, nw, old[u]);
+                }
+            }
+        }
+        return;
+    }
     const unsigned nchunks = (unsigned)((per_colour + 63) >> 6);
     for (;;) {
         unsigned c = 0;

@@ -187,6 +187,41 @@ __device__ __forceinline__ bool big_or_zero(double x) {
     return ((hi & 0x7ff00000) >= (63 << 20)) || (((hi & 0x7fffffff) | lo) == 0);
 }
 
+// big_or_zero of all four: one minimum of the exponent fields for the common case (all at least
+// 2^-960), the zero cases only when that fails.
+__device__ __forceinline__ bool all_big_or_zero(double a, double b, double c, double d) {
+    const unsigned ea = (unsigned)__double2hiint(a) & 0x7ff00000u, eb = (unsigned)__double2hiint(b) & 0x7ff00000u;
+    const unsigned ec = (unsigned)__double2hiint(c) & 0x7ff00000u, ed = (unsigned)__double2hiint(d) & 0x7ff00000u;
+    if (min(min(ea, eb), min(ec, ed)) >= (63u << 20)) return true;
+    return big_or_zero(a) && big_or_zero(b) && big_or_zero(c) && big_or_zero(d);
+}
+
+// The rounding core of the integer multiply: the product of two 53-bit significands mx, mc (with
+// their leading bits) and biased exponents ex, ec, rounded to nearest, ties to even, with the
+// given sign bit. Returns false when the result leaves the normal range.
+__device__ __forceinline__ bool mul_rn_core(unsigned long long sign, int ex, unsigned long long mx, int ec,
+                                            unsigned long long mc, double& out) {
+    const unsigned long long lo = mx * mc;
+    const unsigned long long hi = __umul64hi(mx, mc);  // 2^104 <= hi:lo < 2^106
+    const bool top = (hi >> 41) != 0;                    // the product is >= 2^105
+    int e = ex + ec - 1023 + (top ? 1 : 0);              // biased exponent before rounding
+    if (e <= 0) return false;
+    // round to nearest, ties to even, dropping sh = 52 or 53 bits: add 2^(sh-1) - 1 plus the
+    // lowest kept bit, then truncate (a remainder above half carries, one below does not, and
+    // exactly half carries only from an odd significand)
+    const unsigned long long keep = top ? (lo >> 53) & 1 : (lo >> 52) & 1;
+    const unsigned long long lo2 = lo + (top ? (1ull << 52) - 1 : (1ull << 51) - 1) + keep;
+    const unsigned long long hi2 = hi + (lo2 < lo ? 1 : 0);
+    unsigned long long mant = top ? (hi2 << 11) | (lo2 >> 53) : (hi2 << 12) | (lo2 >> 52);
+    if (mant >> 53) {  // rounded up to 2^53
+        mant >>= 1;
+        ++e;
+    }
+    if (e >= 0x7ff) return false;
+    out = __longlong_as_double((long long)(sign | ((unsigned long long)e << 52) | (mant & ((1ull << 52) - 1))));
+    return true;
+}
+
 // x * c rounded to nearest, ties to even, by integer arithmetic, for a normal constant c (bit
 // pattern cb): the 106-bit product of the two 53-bit significands, its top 53 bits, and the
 // IEEE 754 round-half-to-even rule on the rest. A zero x gives the signed zero. Returns false
@@ -208,31 +243,7 @@ __device__ __forceinline__ bool mul_rn_int(double x, unsigned long long cb, doub
     }
     if (ex == 0x7ff) return false;
     const unsigned long long frac = (1ull << 52) - 1;
-    const unsigned long long mx = (xb & frac) | (1ull << 52);
-    const unsigned long long mc = (cb & frac) | (1ull << 52);
-    const unsigned long long lo = mx * mc;
-    const unsigned long long hi = __umul64hi(mx, mc);  // 2^104 <= hi:lo < 2^106
-    const int top = (int)(hi >> 41);                     // 1 when the product is >= 2^105
-    int e = ex + ec - 1023 + top;                        // biased exponent before rounding
-    if (e <= 0) return false;
-    unsigned long long mant, rem, half;
-    if (top) {
-        mant = (hi << 11) | (lo >> 53);
-        rem = lo & ((1ull << 53) - 1);
-        half = 1ull << 52;
-    } else {
-        mant = (hi << 12) | (lo >> 52);
-        rem = lo & ((1ull << 52) - 1);
-        half = 1ull << 51;
-    }
-    mant += (rem > half || (rem == half && (mant & 1))) ? 1 : 0;
-    if (mant >> 53) {  // rounded up to 2^53
-        mant >>= 1;
-        ++e;
-    }
-    if (e >= 0x7ff) return false;
-    out = __longlong_as_double((long long)(sign | ((unsigned long long)e << 52) | (mant & frac)));
-    return true;
+    return mul_rn_core(sign, ex, (xb & frac) | (1ull << 52), ec, (cb & frac) | (1ull << 52), out);
 }
 
 // c * x as the exact update computes it: on the integer pipes where mul_rn_int applies, on the
@@ -279,6 +290,30 @@ __device__ __forceinline__ double div_rn_const(double a, const DivConst& d) {
     return q;
 }
 
+// k.c * x as mul_rn_int computes it, for a constant prepared on the host (mul_const): its
+// significand, exponent and sign come from the launch parameters. The folded update uses it for
+// its two constants (2048^2: 52.3 vs 52.6 us per sweep); in the general update, with four
+// constants and the division, it ran slower (1536^2: 77.6 vs 60.9 us) and is not used there.
+__device__ __forceinline__ bool mul_rn_int_k(double x, const MulConst& k, double& out) {
+    const unsigned long long xb = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)((xb >> 52) & 0x7ff);
+    if (!k.ok) return false;
+    const unsigned long long sign = (xb & 0x8000000000000000ull) ^ k.sign;
+    if (ex == 0) {
+        if ((xb << 1) != 0) return false;  // subnormal
+        out = __longlong_as_double((long long)sign);
+        return true;
+    }
+    if (ex == 0x7ff) return false;
+    return mul_rn_core(sign, ex, (xb & ((1ull << 52) - 1)) | (1ull << 52), k.e, k.m, out);
+}
+
+__device__ __forceinline__ double mul_rn_k(const MulConst& k, double x) {
+    double r;
+    if (!mul_rn_int_k(x, k, r)) r = __dmul_rn(k.c, x);
+    return r;
+}
+
 // The new value of one cell (no norm).
 template <Arith A, int KIND, bool FOLD>
 __device__ __forceinline__ double point_value(const PoissonParams& p, double up, double dn, double rt,
@@ -291,9 +326,9 @@ __device__ __forceinline__ double point_value(const PoissonParams& p, double up,
             const double s2 = __dadd_rn(rt, lt);
             const double S = __dadd_rn(s1, s2);
             const double t = __dsub_rn(S, g);
-            if (big_or_zero(s1) && big_or_zero(s2) && big_or_zero(S) && big_or_zero(t)) {
+            if (all_big_or_zero(s1, s2, S, t)) {
                 if (KIND == CNV_POISSON_SOR)
-                    nw = __dadd_rn(mul_rn(p.b4, t), mul_rn(p.omb, old));
+                    nw = __dadd_rn(mul_rn_k(p.kb4, t), mul_rn_k(p.komb, old));
                 else
                     nw = __dmul_rn(0.25, t);
             } else {
