@@ -51,7 +51,10 @@ namespace {
 // bound by the FP64 pipe, and the exact integer multiply moves those multiplications to the
 // integer pipes (the same bits). Measured on a GB300 (cnv_time_passes on a developed, smoothed-
 // noise field; ms at 1024^2 / 2048^2): k_pre 0.162 / 0.544 with FP64 multiplies, 0.116 / 0.388
-// with all 28 on the integer pipes; k_post 0.168 / 0.643 and 0.166 / 0.446.
+// with all 28 on the integer pipes; k_post 0.168 / 0.643 and 0.166 / 0.446. With the multiply's
+// cheaper rounding step, all on the integer pipes: k_pre 0.112 / 0.372, k_post 0.137 / 0.439;
+// half on each pipe (first derivatives on one, second derivatives or continuity on the other)
+// ran 0.132-0.134 / 0.437-0.454 and 0.153-0.159 / 0.509-0.521.
 constexpr int kPreD1 = kMulInt;      // k_pre: DX w, DY w
 constexpr int kPreD2 = kMulInt;      // k_pre: DX2 w, DY2 w
 constexpr int kPostVel = kMulInt;    // k_post: DY psi, DX psi
