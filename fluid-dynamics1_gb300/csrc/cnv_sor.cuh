@@ -135,21 +135,17 @@ __device__ __forceinline__ bool norm_add(NormAcc& acc, double nw, double old) {
             const long long sd = (long long)(a - b);
             const unsigned long long d = (unsigned long long)(sd < 0 ? -sd : sd);  // < 2^52
             const int s = e - 995;                                                   // 0 .. 73
-            unsigned long long dl, dh;
-            if (s == 0) {
-                dl = d;
-                dh = 0;
-            } else if (s < 64) {
-                dl = d << s;
-                dh = d >> (64 - s);
-            } else {
-                dl = 0;
-                dh = d << (s - 64);
-            }
-            acc.c[0] += dl & 0xffffffffull;
-            acc.c[1] += dl >> 32;
-            acc.c[2] += dh & 0xffffffffull;
-            acc.c[3] += dh >> 32;
+            // d << s in 32-bit words: d << (s & 31) is three words x0..x2 (funnel shifts), which
+            // land in chunks w, w+1, w+2 for w = s >> 5 (for w = 2, x2 is 0: d << 9 < 2^61)
+            const unsigned d0 = (unsigned)d, d1 = (unsigned)(d >> 32);
+            const int w = s >> 5, r = s & 31;
+            const unsigned x0 = d0 << r;
+            const unsigned x1 = __funnelshift_l(d0, d1, r);
+            const unsigned x2 = __funnelshift_l(d1, 0u, r);
+            acc.c[0] += w == 0 ? x0 : 0u;
+            acc.c[1] += w == 0 ? x1 : (w == 1 ? x0 : 0u);
+            acc.c[2] += w == 0 ? x2 : (w == 1 ? x1 : x0);
+            acc.c[3] += w == 1 ? x2 : (w == 2 ? x1 : 0u);
             return true;
         }
     }
