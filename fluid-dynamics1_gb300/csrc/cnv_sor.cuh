@@ -205,10 +205,14 @@ __device__ __forceinline__ bool mul_rn_core(unsigned long long sign, int ex, uns
     // round to nearest, ties to even, dropping sh = 52 or 53 bits: add 2^(sh-1) - 1 plus the
     // lowest kept bit, then truncate (a remainder above half carries, one below does not, and
     // exactly half carries only from an odd significand)
-    const unsigned long long keep = top ? (lo >> 53) & 1 : (lo >> 52) & 1;
+    const int k = top ? 21 : 20;  // sh - 32: the dropped bits reach into lo's upper word
+    const unsigned long long keep = ((unsigned)(lo >> 32) >> k) & 1u;
     const unsigned long long lo2 = lo + (top ? (1ull << 52) - 1 : (1ull << 51) - 1) + keep;
     const unsigned long long hi2 = hi + (lo2 < lo ? 1 : 0);
-    unsigned long long mant = top ? (hi2 << 11) | (lo2 >> 53) : (hi2 << 12) | (lo2 >> 52);
+    // (hi2:lo2) >> sh from the upper three words by two funnel shifts
+    const unsigned h0 = (unsigned)hi2, h1 = (unsigned)(hi2 >> 32);
+    unsigned long long mant = ((unsigned long long)__funnelshift_r(h0, h1, k) << 32) |
+                              __funnelshift_r((unsigned)(lo2 >> 32), h0, k);
     if (mant >> 53) {  // rounded up to 2^53
         mant >>= 1;
         ++e;
