@@ -188,8 +188,8 @@ class ClockSampler:
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one k_poisson launch on the headline
 # workload, from an ncu capture of the kernel as built at the commit named below. The solve runs
 # from L2, so this is the compulsory first touch of psi and f, not a per-sweep figure.
-POISSON_TRAFFIC = {"bytes_per_launch": 18015232.0,
-                   "source": "ncu capture of k_poisson, 1024^2 workload, one launch (step 0), build of commit 9d3f6e8"}
+POISSON_TRAFFIC = {"bytes_per_launch": 17982464.0,
+                   "source": "ncu capture of k_poisson, 1024^2 workload, one launch (step 0), build of commit f9d9c8a"}
 
 L2_NOTE = "flushed before every timed step on the GPU (256 MB device write)"
 
