@@ -1,8 +1,8 @@
 """The named-barrier sequence of the persistent SOR kernel (csrc/cnv_poisson.cu), checked on the
 CPU by running it under many random schedules.
 
-A block of k_poisson has 16 warps: warps 0-14 update cells (0-3 also the tile's frame) and warp
-15, the signal warp, does the inter-block work. They meet only at named barriers, which cannot
+A block of k_poisson has 32 warps: warps 0-30 update cells (0-11 also the tile's frame) and warp
+31, the signal warp, does the inter-block work. They meet only at named barriers, which cannot
 time out, so the sequence must never pair arrivals of two different instances of one barrier
 (PTX bar semantics: an instance completes when its expected count of warps has arrived, and
 later arrivals count toward the next instance). The model below restates the sequences of
@@ -20,8 +20,10 @@ import random
 
 import pytest
 
-CELL_WARPS, FRAME_WARPS = 15, 4
-EXPECTED = {"DEC": 16, "GO": FRAME_WARPS + 1, "PUB": FRAME_WARPS + 1, "END": CELL_WARPS, "NORM": 16}
+CELL_WARPS, FRAME_WARPS = 31, 12  # kCellWarps, kFrameWarps of csrc/cnv_poisson.cu
+SIGNAL_WARP = CELL_WARPS
+EXPECTED = {"DEC": CELL_WARPS + 1, "GO": FRAME_WARPS + 1, "PUB": FRAME_WARPS + 1, "END": CELL_WARPS,
+            "NORM": CELL_WARPS + 1}
 
 
 def signal_ops(kmax, halves, stop_at, norm_before_go=True):
@@ -66,7 +68,7 @@ def cell_ops(warp, kmax, halves, stop_at):
 def run_schedule(kmax, halves, stop_at, seed, norm_before_go=True):
     """One random interleaving; returns None or a description of what went wrong."""
     rnd = random.Random(seed)
-    gens = {15: signal_ops(kmax, halves, stop_at, norm_before_go)}
+    gens = {SIGNAL_WARP: signal_ops(kmax, halves, stop_at, norm_before_go)}
     for w in range(CELL_WARPS):
         gens[w] = cell_ops(w, kmax, halves, stop_at)
     cur = {w: next(g, None) for w, g in gens.items()}
@@ -123,3 +125,15 @@ def test_kernel_barrier_sequence_never_mispairs(halves):
 def test_old_order_mispairs_for_jacobi():
     bad = failures(1, False, 60)
     assert bad and all("NORM" in r for *_, r in bad)
+
+
+def test_model_matches_the_kernel_layout():
+    """The model's warp counts are the kernel's (kThreads / 32 - 1 cell warps, kFrameWarps)."""
+    import os
+    import re
+
+    src = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "fluid-dynamics1_gb300", "csrc",
+                            "cnv_poisson.cu")).read()
+    threads = int(re.search(r"constexpr int kThreads = (\d+);", src).group(1))
+    frame = int(re.search(r"constexpr int kFrameWarps = (\d+);", src).group(1))
+    assert (threads // 32 - 1, frame) == (CELL_WARPS, FRAME_WARPS)
