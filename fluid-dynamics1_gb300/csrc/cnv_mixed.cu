@@ -132,6 +132,10 @@ __device__ __noinline__ void mixed_half_sweep(int sc_off, int so_off, int rq_off
         const int mlo = floor_half(lo_c - q + 1), mhi = floor_half(hi_c - 1 - q);
         const int row = (i - sr0) * swm - m0;
         const float* rqrow = rq + (size_t)i * P;
+        // unrolled 4 deep where R/den comes from L2 (the large grids): 2048^2 8.87 vs 9.18 us per
+        // sweep; with R/den in shared memory (1024^2) unrolling ran slower (3.50 vs 3.46), and the
+        // batch kernel's strip sweep, the same loop, ran its step 24 % slower unrolled
+#pragma unroll(RQ_SMEM ? 1 : 4)
         for (int m = mlo + lane; m <= mhi; m += 32) {
             const int k = row + m;
             const float up = mx_smem[so_off + k + swm], dn = mx_smem[so_off + k - swm];
